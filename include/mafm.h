@@ -1,0 +1,241 @@
+/*
+ * mafm.h — C ABI of libmafm, the GB300 (sm_103a) implementation of the
+ * MechAFM scan hot path.
+ *
+ * The reference (SINGROUP/MechAFM) has no library interface: its scan runs
+ * inside one process (`mechafm-omp INPUT [OUTPUT]`, src/mechafm.cpp:209-233).
+ * Its in-process seams are
+ *   int FIREMinimisation(System&, const InputOptions&)        src/minimiser.hpp:23
+ *   int SDMinimisation(System&, const InputOptions&)          src/minimiser.hpp:20
+ *   void Interaction::eval(positions, forces, energies)       src/interactions.hpp:72
+ * called per pixel from Simulation::run (src/simulation.cpp:67-143).  They
+ * are too fine-grained for a GPU, so this ABI cuts one level higher: "relax
+ * every pixel column of a scan".  Each entry point below names the reference
+ * code it replaces.
+ *
+ * Conventions
+ *   - Every function returns int status, 0 (MAFM_OK) on success.  No C++
+ *     exception crosses this boundary.  mafm_last_error() gives the message
+ *     of the last failure on the calling thread; for input-file errors it is
+ *     the reference's own error() text (src/messages.cpp:12-27).
+ *   - Plain pointers and sizes only.  Buffers passed in are owned by the
+ *     caller; the library copies what it keeps.
+ *   - Units are the reference's: Angstrom, energy unit chosen by `units`,
+ *     charges in e.
+ *   - `stream` is a cudaStream_t passed as void* (NULL = legacy default stream).
+ */
+#ifndef MAFM_H
+#define MAFM_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MAFM_ABI_VERSION 1
+
+/* ---- status codes ------------------------------------------------------- */
+enum {
+    MAFM_OK = 0,
+    MAFM_E_INVALID = 1,     /* bad argument or descriptor */
+    MAFM_E_IO = 2,          /* file missing or unreadable */
+    MAFM_E_PARSE = 3,       /* input/xyz/parameter/cube file error (reference error()) */
+    MAFM_E_CUDA = 4,        /* CUDA runtime or launch failure */
+    MAFM_E_NOMEM = 5,       /* device or host allocation failed */
+    MAFM_E_RANGE = 6,       /* a size beyond a documented limit */
+    MAFM_E_DEVICE = 7,      /* device-side error word set (bounded wait expired) */
+    MAFM_E_UNSUPPORTED = 8  /* option combination not implemented on the GPU */
+};
+
+/* ---- enumerations mirroring the reference ------------------------------- */
+enum { MAFM_MIN_SD = 0, MAFM_MIN_FIRE = 1 };                 /* minimiser.hpp:10-13 */
+enum { MAFM_INT_EULER = 0, MAFM_INT_MIDPOINT = 1, MAFM_INT_RK4 = 2 }; /* integrators.hpp:4-8 */
+enum { MAFM_TERM_E = 0, MAFM_TERM_F = 1, MAFM_TERM_EF = 2 };  /* simulation.hpp:21 */
+enum { MAFM_PAIR_LJ = 0, MAFM_PAIR_MORSE = 1 };               /* interactions.hpp:79-119 */
+enum { MAFM_UNITS_KCAL = 0, MAFM_UNITS_KJ = 1, MAFM_UNITS_EV = 2 }; /* simulation.hpp:27 */
+
+/* Arithmetic of a run. */
+enum {
+    MAFM_FP64 = 0,   /* plain FP64, the reference's operation order */
+    MAFM_FP32C = 1   /* FP32 pair math, compensated sums, FP64 energy check */
+};
+
+/* Per-point status bits (mafm_point.status). */
+enum {
+    MAFM_PT_MAXSTEPS = 1,   /* minimiser returned maxsteps without converging */
+    MAFM_PT_NONFINITE = 2,  /* a force or energy was NaN/Inf */
+    MAFM_PT_OUTSIDE = 4     /* rigid grid lookup clamped at the border
+                               (reference warns, force_grid.cpp:181-217) */
+};
+
+/* One tip–atom van der Waals pair.  LJ: p = {es6, es12, 0} with
+ * es6 = 4 eps sig^6 and es12 = 4 eps sig^12 (simulation.cpp:245-246,263-264).
+ * Morse: p = {De, a, re} (interactions.cpp:29-40). */
+typedef struct mafm_pair {
+    int32_t kind;
+    int32_t reserved;
+    double p[3];
+} mafm_pair;
+
+/*
+ * Everything one scan needs, after the reference's host-side preparation
+ * (Simulation::initialize, simulation.cpp:31-65): parsed options, surface
+ * atoms centred and shifted (system.cpp:103-136), tip–dummy distance
+ * (simulation.cpp:218-225), pair parameters mixed and overwritten
+ * (simulation.cpp:227-267).  mafm_input_desc() fills one from input files.
+ */
+typedef struct mafm_scan_desc {
+    /* surface atoms (System index 2.. in the reference) */
+    int32_t n_atoms;
+    int32_t n_types;
+    const double* pos;          /* [n_atoms*3] x,y,z */
+    const double* charge;       /* [n_atoms] Coulomb charge (xyz or parameter file,
+                                   parse.cpp:571-584 and simulation.cpp:273-289) */
+    const int32_t* type;        /* [n_atoms] index into tip_pair */
+    const mafm_pair* tip_pair;  /* [n_types] tip–type pair */
+    mafm_pair dummy_pair;       /* dummy–tip pair (buildTipDummyInteractions) */
+    double tip_charge;
+    double dummy_charge;
+    double qbase;               /* Coulomb prefactor of the unit system (parse.cpp:278-298) */
+    int32_t coulomb;            /* tip–surface Coulomb (off under vdw_pbc) */
+    int32_t tip_dummy_coulomb;
+    double harm_k;              /* TipHarmonicInteraction k, r0 (interactions.cpp:252-266) */
+    double harm_r0;
+    double tip_dummy_d;         /* initial dummy–tip z distance */
+    /* periodicity (simulation.cpp:39-59, 297-312; system.cpp:139-162) */
+    int32_t vdw_pbc;            /* sum 3x3 in-plane images of every atom */
+    int32_t tip_pbc;            /* wrap pixel xy into the cell (setDummyXY) */
+    double cell[9];             /* row-major; columns are the cell vectors */
+    double offset[3];           /* System offset of the centring / z shift */
+    /* scan geometry (mechafm.cpp:47-49, simulation.cpp:78-122) */
+    int32_t nx, ny, nz;
+    int32_t reserved0;
+    double dx, dy, dz;
+    double zhigh, zlow;
+    double area[2];
+    /* minimiser (simulation.hpp:50-59) */
+    int32_t minimiser;
+    int32_t integrator;
+    int32_t minterm;
+    int32_t maxsteps;
+    double etol, ftol, dt;
+    /* rigid force grid (simulation.cpp:420-501) */
+    int32_t rigidgrid;
+    /* external Hartree field (simulation.cpp:322-417), values already scaled to
+       the energy unit and the origin already shifted by the System offset */
+    int32_t use_external_potential;
+    const double* epot;         /* [n0*n1*n2], index (i*n1 + j)*n2 + k */
+    int32_t epot_n[3];
+    int32_t reserved1;
+    double epot_basis[9];       /* row-major; columns are the voxel vectors */
+    double epot_origin[3];
+} mafm_scan_desc;
+
+/* One relaxed pixel·z point.  Point index p = (i*ny + j)*nz + k for pixel
+ * (i, j) and height k, as OutputData.indices (simulation.cpp:117-119). */
+typedef struct mafm_point {
+    double tip[3];      /* relaxed tip position, System::positions_[1] */
+    double force[3];    /* tip–surface force at the relaxed position (system.cpp:41-51) */
+    double energy;      /* tip–surface energy */
+    int32_t steps;      /* value returned by the minimiser (minimiser.cpp:79-80,128) */
+    int32_t status;     /* MAFM_PT_* bits */
+} mafm_point;
+
+typedef struct mafm_run_opts {
+    int32_t precision;          /* MAFM_FP64 or MAFM_FP32C */
+    int32_t lanes_per_column;   /* FP32C: 1,2,4,8,16,32 lanes share a column; 0 = tuned */
+    int32_t block_threads;      /* 0 = default */
+    int32_t columns_per_tile;   /* FP32C: warp work-tile size in columns; 0 = default */
+    int32_t col_begin;          /* relax only columns [col_begin, col_end) of */
+    int32_t col_end;            /*   i*ny + j; 0,0 = all */
+} mafm_run_opts;
+
+typedef struct mafm_run_stats {
+    uint64_t total_steps;       /* sum of mafm_point.steps (statistics.txt, mechafm.cpp:140-152) */
+    uint64_t force_evals;       /* tip force evaluations, output evaluations included */
+    uint64_t pair_evals;        /* tip–atom pair terms evaluated (vdW + Coulomb) */
+    uint32_t error_word;        /* OR of MAFM_PT_* over all points, plus device error bits */
+    uint32_t reserved;
+    double kernel_ms;           /* device time of the relax kernel(s) */
+} mafm_run_stats;
+
+typedef struct mafm_input mafm_input;   /* parsed input files + prepared System */
+typedef struct mafm_scan mafm_scan;     /* device-resident scan */
+
+/* ---- errors / version ---------------------------------------------------- */
+const char* mafm_last_error(void);
+int mafm_abi_version(void);
+
+/* ---- input front-end (host) ---------------------------------------------
+ * Replaces readInputFile / readXYZFile / readParameterFile (parse.cpp:83-782,
+ * src/parse.hpp:5-10), CubeReader (cube_io.cpp:10-139) and the host part of
+ * Simulation::initialize (simulation.cpp:31-65).  verbose != 0 prints the
+ * reference's banner, option echo and warnings (parse.cpp:32-38,407-472). */
+int mafm_input_load(const char* input_file, int verbose, mafm_input** out);
+/* Fill a descriptor whose pointers refer to storage owned by `in`. */
+int mafm_input_desc(const mafm_input* in, mafm_scan_desc* out);
+/* Output options of the input file: gzip, statistics, bufsize. */
+int mafm_input_output_opts(const mafm_input* in, int32_t* gzip, int32_t* statistics,
+                           int32_t* bufsize);
+int mafm_input_free(mafm_input* in);
+
+/* ---- device scan ----------------------------------------------------------
+ * Uploads atoms and parameters, then builds what the reference builds in
+ * buildInteractions (simulation.cpp:201-216): the external field by FFT
+ * (ElectrostaticPotentialInteraction ctor, interactions.cpp:53-234) and the
+ * rigid force grid (buildTipGridInteractions, simulation.cpp:420-501), in
+ * FP64 for MAFM_FP64 runs and in FP32 for MAFM_FP32C runs.
+ * device < 0 uses the current device. */
+int mafm_scan_create(int device, const mafm_scan_desc* desc, mafm_scan** out);
+int mafm_scan_destroy(mafm_scan* scan);
+/* Number of points nx*ny*nz and columns nx*ny of the scan. */
+int mafm_scan_size(const mafm_scan* scan, int64_t* n_points, int64_t* n_columns);
+
+/* Relax every point of the scan: the pixel/z loops of Simulation::run
+ * (simulation.cpp:78-122) with FIREMinimisation / SDMinimisation
+ * (minimiser.cpp:39-129), the integrators (integrators.cpp:8-111) and
+ * System::getOutput (system.cpp:28-51).  `out` holds n_points records and
+ * may be host or device memory; for host memory the call copies the result
+ * back and returns after the copy.  `stats` may be NULL; when given, the
+ * call synchronises the stream. */
+int mafm_run(mafm_scan* scan, const mafm_run_opts* opts, mafm_point* out,
+             mafm_run_stats* stats, void* stream);
+
+/* Relax several scans in one persistent launch (MAFM_FP32C only).  outs[s]
+ * receives scan s's points; all outs must be device memory, or all host. */
+int mafm_run_batch(mafm_scan* const* scans, int32_t n_scans, const mafm_run_opts* opts,
+                   mafm_point* const* outs, mafm_run_stats* stats, void* stream);
+
+/* Evaluate the tip–surface force and energy at n given tip positions
+ * (System::evalTipSurfaceForces, system.cpp:41-51): pairs, external field or
+ * rigid grid, whatever the scan uses.  what: 0 = all tip–surface terms,
+ * 1 = external field only.  pts[n*3] and out[n*4] = {Fx,Fy,Fz,E} are host
+ * memory.  precision selects the FP64 or FP32 tables. */
+int mafm_scan_sample(mafm_scan* scan, int32_t precision, int32_t what,
+                     const double* pts, int64_t n, double* out);
+
+/* Geometry of the rigid force grid (or of the external field when what = 1):
+ * node counts, basis (row-major, columns = steps) and origin. */
+int mafm_scan_grid_info(const mafm_scan* scan, int32_t what, int32_t n[3],
+                        double basis[9], double origin[3]);
+/* Copy the FP64 grid nodes {Fx,Fy,Fz,E} (n0*n1*n2*4 doubles, z fastest). */
+int mafm_scan_grid_copy(const mafm_scan* scan, int32_t what, double* out);
+
+/* ---- output (host) ---------------------------------------------------------
+ * Writes scan-%06.3f.dat[.gz] files and statistics.txt exactly as the
+ * reference (openUniverse mechafm.cpp:60-75, writeOutput simulation.cpp:145-199,
+ * finalize mechafm.cpp:140-152).  folder may be "" (current directory) and
+ * must end in '/' otherwise.  Rows are written in point order. */
+int mafm_write_output(const mafm_input* in, const mafm_point* pts, const char* folder,
+                      int32_t gzip);
+/* statistics.txt of finalize (mechafm.cpp:140-152). */
+int mafm_write_statistics(const mafm_input* in, const char* folder, uint64_t total_steps,
+                          double wall_s, double total_s);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MAFM_H */

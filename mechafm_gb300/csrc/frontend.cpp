@@ -1,0 +1,989 @@
+// frontend.cpp — host side of the drop-in boundary: the reference's input,
+// xyz, parameter and cube readers, the System preparation of
+// Simulation::initialize, pair-parameter resolution, and the scan-file writer.
+//
+// Behaviour (defaults, keywords, error texts, warnings, output formats) follows
+// the reference so that `mechafm-gpu` is a drop-in for `mechafm-omp`:
+//   readInputFile        parse.cpp:83-474
+//   readXYZFile          parse.cpp:477-585
+//   readParameterFile    parse.cpp:588-697 (+ readFlexibleParameters :699-782)
+//   CubeReader           cube_io.cpp:10-139
+//   Simulation::initialize / build*Interactions   simulation.cpp:31-65, 201-515
+//   writeOutput / openUniverse / finalize          simulation.cpp:145-199,
+//                                                  mechafm.cpp:37-80, 103-154
+// Everything here is compiled with -ffp-contract=off: the reference is built
+// for x86-64 without FMA, and the host arithmetic (centring, mixing, matrix
+// inverse) must give the same bits on an aarch64 host.
+#include <cctype>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "mafm_internal.h"
+
+namespace mafm {
+
+static thread_local std::string g_last_error;
+
+void set_last_error(const std::string& msg) { g_last_error = msg; }
+
+void fail(int code, const char* fmt, ...) {
+    char buf[1024];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    throw Failure{code, buf};
+}
+
+namespace {
+
+constexpr int kLine = 512;    // LINE_LENGTH (globals.hpp:6)
+constexpr double kPi = 3.14159265358979323846;       // globals.hpp:10
+constexpr double kSixthRoot2 = 1.12246204830937298142;  // globals.hpp:11
+constexpr double kTolerance = 1e-10;                 // globals.hpp:8
+constexpr double kBohr = 0.52917721092;              // cube_io.hpp:17
+constexpr double kHartreeEV = 27.211386;             // globals.hpp:20-22
+constexpr double kHartreeKJ = 2625.5002;
+constexpr double kHartreeKcal = 627.50961;
+
+enum Normal { NORMAL_X, NORMAL_Y, NORMAL_Z };
+
+struct AtomParams {
+    double eps = 0, sig = 0, q = 0, mass = 0;
+};
+
+struct Overwrite {
+    std::string a, b;
+    bool morse = false;
+    double eps = 0, sig = 0, de = 0, alpha = 0, re = 0;
+};
+
+bool is_comment(const char* line) {
+    return line[0] == '#' || line[0] == '%' || line[0] == '\n';
+}
+
+void lower(char* s) {
+    for (; *s; ++s) *s = (char)tolower((unsigned char)*s);
+}
+
+bool is_int(const char* s) {
+    for (; *s; ++s)
+        if (!(isdigit((unsigned char)*s) || *s == '-' || *s == '+')) return false;
+    return true;
+}
+
+int count_columns(const char* line) {
+    char buf[kLine];
+    snprintf(buf, sizeof buf, "%s", line);
+    int n = 0;
+    for (char* t = strtok(buf, " \t\n\r\f"); t; t = strtok(nullptr, " \t\n\r\f")) ++n;
+    return n;
+}
+
+bool multiset_eq(const std::string& a, const std::string& b, const std::string& c,
+                 const std::string& d) {
+    return (a == c && b == d) || (a == d && b == c);
+}
+
+// 3x3 helpers with the reference's operation order (matrices.hpp:89-160).
+struct M3 {
+    double v[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+    double det() const {
+        double d = 0;
+        d = v[0][0] * (v[1][1] * v[2][2] - v[1][2] * v[2][1]);
+        d += v[0][1] * (v[1][2] * v[2][0] - v[1][0] * v[2][2]);
+        d += v[0][2] * (v[1][0] * v[2][1] - v[1][1] * v[2][0]);
+        return d;
+    }
+    M3 inverse() const {
+        M3 r;
+        double inv_det = 1 / det();
+        double a = v[0][0], b = v[0][1], c = v[0][2];
+        double d = v[1][0], e = v[1][1], f = v[1][2];
+        double g = v[2][0], h = v[2][1], i = v[2][2];
+        r.v[0][0] = inv_det * (e * i - f * h);
+        r.v[0][1] = -inv_det * (b * i - c * h);
+        r.v[0][2] = inv_det * (b * f - c * e);
+        r.v[1][0] = -inv_det * (d * i - f * g);
+        r.v[1][1] = inv_det * (a * i - c * g);
+        r.v[1][2] = -inv_det * (a * f - c * d);
+        r.v[2][0] = inv_det * (d * h - e * g);
+        r.v[2][1] = -inv_det * (a * h - b * g);
+        r.v[2][2] = inv_det * (a * e - b * d);
+        return r;
+    }
+    M3 mul(const M3& o) const {
+        M3 r;
+        for (int i = 0; i < 3; i++)
+            for (int j = 0; j < 3; j++)
+                for (int k = 0; k < 3; k++) r.v[i][j] += v[i][k] * o.v[k][j];
+        return r;
+    }
+    M3 transpose() const {
+        M3 r;
+        for (int i = 0; i < 3; i++)
+            for (int j = 0; j < 3; j++) r.v[i][j] = v[j][i];
+        return r;
+    }
+};
+
+}  // namespace
+}  // namespace mafm
+
+// The opaque input handle of the C ABI.
+struct mafm_input {
+    // --- options (InputOptions, simulation.hpp:30-60) ---
+    std::string inputfolder, inputfile, xyzfile, paramfile, e_potential_file;
+    std::string tipatom, dummyatom;
+    double area[2] = {10, 10}, center[2] = {-1, -1};
+    double dx = 0.1, dy = 0.1, dz = 0.1, zlow = 6.0, zhigh = 10.0;
+    bool vdw_pbc = false;
+    double cell_a[3] = {0, 0, 0}, cell_b[3] = {0, 0, 0}, cell_c[3] = {0, 0, 0};
+    int normal = mafm::NORMAL_Z;
+    int units = MAFM_UNITS_KCAL;
+    bool coulomb = false, tip_dummy_coulomb = false, use_external_potential = false;
+    int maxsteps = 5000;
+    int minterm = -1;
+    double etol = 0.01, ftol = 0.01, dt = 0.001;
+    int bufsize = 1000;
+    bool gzip = true, statistics = false, flexible = false, rigidgrid = false;
+    bool xyz_charges = false;
+    int minimiser = MAFM_MIN_FIRE, integrator = MAFM_INT_MIDPOINT;
+    // --- interaction parameters (InteractionParameters, interactions.hpp:47-55) ---
+    // qbase is only assigned by a `units` line in the reference (parse.cpp:278-298);
+    // without one it is left uninitialised there.  Here it starts at the kcal/mol value.
+    double qbase = 332.06371;
+    double harm_k = 0, harm_r0 = 0;
+    double bond_k = 0, angle_k = 0, dihedral_k = 0;
+    double sub_eps = 0, sub_sig = 0, sub_lambda = 0, sub_rc = 0, sub_k = 0;
+    std::map<std::string, mafm::AtomParams> ap;
+    std::vector<mafm::Overwrite> ow;
+    // --- System (system.hpp:13-77); index 0 dummy, 1 tip, 2.. surface ---
+    int n_atoms = 0;   // including tip and dummy
+    std::vector<std::string> types;
+    std::vector<double> pos;      // 3 per atom
+    std::vector<double> charges;
+    std::vector<int> fixed;
+    double offset[3] = {0, 0, 0};
+    double tip_dummy_d = 0;
+    mafm::M3 cell;
+    bool tip_pbc = false;
+    int np[3] = {0, 0, 0};
+    // --- descriptor storage ---
+    std::vector<double> d_pos, d_charge;
+    std::vector<int32_t> d_type;
+    std::vector<mafm_pair> d_pairs;
+    std::vector<std::string> type_names;
+    mafm_pair dummy_pair{};
+    double tip_q_eff = 0, dummy_q_eff = 0;
+    std::vector<double> epot;
+    int epot_n[3] = {0, 0, 0};
+    mafm::M3 epot_basis;
+    double epot_origin[3] = {0, 0, 0};
+    bool verbose = false;
+};
+
+namespace mafm {
+namespace {
+
+void pretty(const mafm_input& in, const char* fmt, ...) {
+    if (!in.verbose) return;
+    char buf[2048];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    fprintf(stdout, "+- %s\n", buf);
+}
+
+void warn(const mafm_input& in, const char* fmt, ...) {
+    if (!in.verbose) return;
+    char buf[2048];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    fprintf(stderr, "+- WARNING: %s\n", buf);
+}
+
+bool on_off(const char* keyword, const char* value) {
+    if (strcmp(value, "on") == 0) return true;
+    if (strcmp(value, "off") == 0) return false;
+    fail(MAFM_E_PARSE, "Option %s must be either on or off!", keyword);
+}
+
+// readInputFile, parse.cpp:83-474.
+void read_input(mafm_input& in) {
+    FILE* fp = fopen(in.inputfile.c_str(), "r");
+    if (!fp) fail(MAFM_E_IO, "The file %s does not exist!", in.inputfile.c_str());
+    struct Closer { FILE* f; ~Closer() { fclose(f); } } closer{fp};
+    char line[kLine], keyword[128] = "", value[128] = "", dump[kLine];
+    char tmp_units[128] = "kcal/mol", tmp_normal[128] = "z", tmp_minterm[128] = "";
+    while (fgets(line, kLine, fp)) {
+        if (is_comment(line)) continue;
+        sscanf(line, "%127s %127s", keyword, value);
+        lower(keyword);
+        if (!strcmp(keyword, "xyzfile")) in.xyzfile = in.inputfolder + value;
+        else if (!strcmp(keyword, "paramfile")) in.paramfile = in.inputfolder + value;
+        else if (!strcmp(keyword, "e_potential_file")) in.e_potential_file = in.inputfolder + value;
+        else if (!strcmp(keyword, "tipatom")) in.tipatom = value;
+        else if (!strcmp(keyword, "dummyatom")) in.dummyatom = value;
+        else if (!strcmp(keyword, "area")) sscanf(line, "%s %lf %lf", dump, &in.area[0], &in.area[1]);
+        else if (!strcmp(keyword, "center")) sscanf(line, "%s %lf %lf", dump, &in.center[0], &in.center[1]);
+        else if (!strcmp(keyword, "zhigh")) in.zhigh = atof(value);
+        else if (!strcmp(keyword, "zlow")) in.zlow = atof(value);
+        else if (!strcmp(keyword, "dx")) in.dx = atof(value);
+        else if (!strcmp(keyword, "dy")) in.dy = atof(value);
+        else if (!strcmp(keyword, "dz")) in.dz = atof(value);
+        else if (!strcmp(keyword, "cell_a")) sscanf(line, "%s %lf %lf %lf", dump, &in.cell_a[0], &in.cell_a[1], &in.cell_a[2]);
+        else if (!strcmp(keyword, "cell_b")) sscanf(line, "%s %lf %lf %lf", dump, &in.cell_b[0], &in.cell_b[1], &in.cell_b[2]);
+        else if (!strcmp(keyword, "cell_c")) sscanf(line, "%s %lf %lf %lf", dump, &in.cell_c[0], &in.cell_c[1], &in.cell_c[2]);
+        else if (!strcmp(keyword, "etol")) in.etol = atof(value);
+        else if (!strcmp(keyword, "ftol")) in.ftol = atof(value);
+        else if (!strcmp(keyword, "dt")) in.dt = atof(value);
+        else if (!strcmp(keyword, "maxsteps")) in.maxsteps = atoi(value);
+        else if (!strcmp(keyword, "bufsize")) in.bufsize = atoi(value);
+        else if (!strcmp(keyword, "gzip")) in.gzip = on_off(keyword, value);
+        else if (!strcmp(keyword, "statistics")) in.statistics = on_off(keyword, value);
+        else if (!strcmp(keyword, "flexible")) in.flexible = on_off(keyword, value);
+        else if (!strcmp(keyword, "rigidgrid")) in.rigidgrid = on_off(keyword, value);
+        else if (!strcmp(keyword, "coulomb")) in.coulomb = on_off(keyword, value);
+        else if (!strcmp(keyword, "tip_dummy_coulomb")) in.tip_dummy_coulomb = on_off(keyword, value);
+        else if (!strcmp(keyword, "use_external_potential")) in.use_external_potential = on_off(keyword, value);
+        else if (!strcmp(keyword, "vdw_pbc")) in.vdw_pbc = on_off(keyword, value);
+        else if (!strcmp(keyword, "surface_normal")) {
+            lower(value);
+            if (!strcmp(value, "z")) in.normal = NORMAL_Z;
+            else if (!strcmp(value, "y")) in.normal = NORMAL_Y;
+            else if (!strcmp(value, "x")) in.normal = NORMAL_X;
+            else fail(MAFM_E_PARSE, "Option %s must be either X, Y or Z!", keyword);
+            snprintf(tmp_normal, sizeof tmp_normal, "%s", value);
+        } else if (!strcmp(keyword, "minterm")) {
+            if (!strcmp(value, "e")) in.minterm = MAFM_TERM_E;
+            else if (!strcmp(value, "f")) in.minterm = MAFM_TERM_F;
+            else if (!strcmp(value, "ef")) in.minterm = MAFM_TERM_EF;
+            else fail(MAFM_E_PARSE, "Option %s must be either e, f or ef!", keyword);
+            snprintf(tmp_minterm, sizeof tmp_minterm, "%s", value);
+        } else if (!strcmp(keyword, "units")) {
+            const double epermv = 1.0;
+            if (!strcmp(value, "kcal/mol") || !strcmp(value, "kcal")) {
+                in.units = MAFM_UNITS_KCAL;
+                in.qbase = 332.06371 / epermv;
+            } else if (!strcmp(value, "kJ/mol") || !strcmp(value, "kJ")) {
+                in.units = MAFM_UNITS_KJ;
+                in.qbase = 1389.354563 / epermv;
+            } else if (!strcmp(value, "eV")) {
+                in.units = MAFM_UNITS_EV;
+                in.qbase = 14.39964901 / epermv;
+            } else {
+                fail(MAFM_E_PARSE, "Option %s must be either kcal/mol (default), kJ/mol or eV!", keyword);
+            }
+            snprintf(tmp_units, sizeof tmp_units, "%s", value);
+        } else if (!strcmp(keyword, "minimiser")) {
+            if (!strcmp(value, "SD")) in.minimiser = MAFM_MIN_SD;
+            else if (!strcmp(value, "FIRE")) in.minimiser = MAFM_MIN_FIRE;
+            else fail(MAFM_E_PARSE, "Unrecognised minimiser type!");
+        } else if (!strcmp(keyword, "integrator")) {
+            if (!strcmp(value, "euler")) in.integrator = MAFM_INT_EULER;
+            else if (!strcmp(value, "midpoint")) in.integrator = MAFM_INT_MIDPOINT;
+            else if (!strcmp(value, "rk4")) in.integrator = MAFM_INT_RK4;
+            else fail(MAFM_E_PARSE, "Unrecognised integrator type!");
+        } else {
+            fail(MAFM_E_PARSE, "Unknown option %s!", keyword);
+        }
+    }
+    if (in.xyzfile.empty()) fail(MAFM_E_PARSE, "Specify at least an xyzfile!");
+    if (in.paramfile.empty()) fail(MAFM_E_PARSE, "Specify at least a parameter file!");
+    if (in.tipatom.empty()) fail(MAFM_E_PARSE, "Specify at least a tip atom!");
+    if (in.dummyatom.empty()) fail(MAFM_E_PARSE, "Specify at least a dummy atom!");
+    if (in.minterm < 0)
+        fail(MAFM_E_PARSE, "Specify at least a minimization termination criterion (e, f, or ef)!");
+    if (in.center[0] == -1 && in.center[1] == -1) {
+        in.center[0] = in.area[0] / 2;
+        in.center[1] = in.area[1] / 2;
+    }
+    // Sanity checks, parse.cpp:386-405.
+    if (in.rigidgrid && in.flexible)
+        fail(MAFM_E_PARSE, "Cannot use a flexible molecule with a static force grid!");
+    if (in.coulomb && in.use_external_potential)
+        fail(MAFM_E_PARSE, "Cannot use Coulomb interaction and external electrostatic potential at the same time!");
+    if (in.use_external_potential && in.flexible)
+        fail(MAFM_E_PARSE, "External potential can be used only for non-flexible systems!");
+    if (in.use_external_potential && in.e_potential_file.empty())
+        fail(MAFM_E_PARSE, "If you want to use external electrostatic potential, you must specify a file that contains it!");
+    if (in.vdw_pbc && in.coulomb)
+        fail(MAFM_E_PARSE, "Implementation of Coulomb interaction does not support any periodic boundary conditions! Use periodic external electrostatic potential instead.");
+    auto zero3 = [](const double* v) { return v[0] == 0 && v[1] == 0 && v[2] == 0; };
+    if (in.vdw_pbc && !in.use_external_potential &&
+        (zero3(in.cell_a) || zero3(in.cell_b) || zero3(in.cell_c)))
+        fail(MAFM_E_PARSE, "The unit cell vectors must be given if periodic vdW is used.");
+
+    // Option echo, parse.cpp:408-472.
+    auto oo = [](bool b) { return b ? "on" : "off"; };
+    pretty(in, "");
+    pretty(in, "Input settings for        %s:", in.inputfile.c_str());
+    pretty(in, "");
+    pretty(in, "xyzfile:                  %-s", in.xyzfile.c_str());
+    pretty(in, "paramfile:                %-s", in.paramfile.c_str());
+    pretty(in, "tipatom:                  %-s", in.tipatom.c_str());
+    pretty(in, "dummyatom:                %-s", in.dummyatom.c_str());
+    pretty(in, "");
+    pretty(in, "units:                    %-s", tmp_units);
+    pretty(in, "");
+    pretty(in, "minterm:                  %-s", tmp_minterm);
+    pretty(in, "etol:                     %-8.4f", in.etol);
+    pretty(in, "ftol:                     %-8.4f", in.ftol);
+    pretty(in, "dt:                       %-8.4f", in.dt);
+    pretty(in, "maxsteps:                 %-8d", in.maxsteps);
+    pretty(in, "");
+    pretty(in, "area:                     %-8.4f %-8.4f", in.area[0], in.area[1]);
+    pretty(in, "center:                   %-8.4f %-8.4f", in.center[0], in.center[1]);
+    pretty(in, "zhigh:                    %-8.4f", in.zhigh);
+    pretty(in, "zlow:                     %-8.4f", in.zlow);
+    pretty(in, "dx:                       %-8.4f", in.dx);
+    pretty(in, "dy:                       %-8.4f", in.dy);
+    pretty(in, "dz:                       %-8.4f", in.dz);
+    pretty(in, "");
+    pretty(in, "surface_normal:           %-s", tmp_normal);
+    pretty(in, "vdw_pbc:                  %-s", oo(in.vdw_pbc));
+    if (in.vdw_pbc && !in.use_external_potential) {
+        pretty(in, "cell_a:                   %-8.4f %-8.4f %-8.4f", in.cell_a[0], in.cell_a[1], in.cell_a[2]);
+        pretty(in, "cell_b:                   %-8.4f %-8.4f %-8.4f", in.cell_b[0], in.cell_b[1], in.cell_b[2]);
+        pretty(in, "cell_c:                   %-8.4f %-8.4f %-8.4f", in.cell_c[0], in.cell_c[1], in.cell_c[2]);
+    }
+    pretty(in, "");
+    pretty(in, "coulomb:                  %-s", oo(in.coulomb));
+    pretty(in, "tip_dummy_coulomb:        %-s", oo(in.tip_dummy_coulomb));
+    pretty(in, "use_external_potential:   %-s", oo(in.use_external_potential));
+    if (in.use_external_potential)
+        pretty(in, "e_potential_file:         %-s", in.e_potential_file.c_str());
+    pretty(in, "");
+    pretty(in, "flexible:                 %-s", oo(in.flexible));
+    pretty(in, "rigidgrid:                %-s", oo(in.rigidgrid));
+    pretty(in, "");
+    pretty(in, "minimiser:         %-s", in.minimiser == MAFM_MIN_SD ? "SD" : "FIRE");
+    static const char* integ[] = {"euler", "midpoint", "rk4"};
+    pretty(in, "integrator:        %-s", integ[in.integrator]);
+    pretty(in, "");
+    pretty(in, "bufsize:           %-8d", in.bufsize);
+    pretty(in, "gzip:              %-s", oo(in.gzip));
+    pretty(in, "statistics:        %-s", oo(in.statistics));
+    pretty(in, "");
+}
+
+// readXYZFile, parse.cpp:477-585.
+void read_xyz(mafm_input& in) {
+    FILE* fp = fopen(in.xyzfile.c_str(), "r");
+    if (!fp) fail(MAFM_E_IO, "No such file: %s!", in.xyzfile.c_str());
+    struct Closer { FILE* f; ~Closer() { fclose(f); } } closer{fp};
+    char line[kLine], value[128] = "";
+    int n = 0;
+    bool firstline = true, realxyz = false;
+    while (fgets(line, kLine, fp)) {
+        if (is_comment(line)) continue;
+        if (firstline) {
+            sscanf(line, "%127s", value);
+            if (is_int(value)) {
+                n = atoi(value);
+                realxyz = true;
+                break;
+            }
+            firstline = false;
+        }
+        if (!firstline) n++;
+    }
+    rewind(fp);
+    if (n < 0) fail(MAFM_E_PARSE, "Invalid number of atoms in the xyz file.");
+    in.n_atoms = n + 2;
+    in.types.assign(in.n_atoms, "");
+    in.pos.assign(3 * (size_t)in.n_atoms, 0.0);
+    in.charges.assign(in.n_atoms, 0.0);
+    in.fixed.assign(in.n_atoms, 0);
+    in.fixed[0] = 1;
+    in.fixed[1] = 0;
+    in.types[0] = in.dummyatom;
+    in.types[1] = in.tipatom;
+    int atom_i = 2, skipped = 0, ncols = 0;
+    firstline = true;
+    while (fgets(line, kLine, fp)) {
+        if (realxyz && skipped < 2) {
+            skipped++;
+            continue;
+        }
+        if (is_comment(line)) continue;
+        if (firstline) {
+            ncols = count_columns(line);
+            firstline = false;
+        }
+        char type[64] = "";
+        double x = 0, y = 0, z = 0, q = 0;
+        int fx = 0;
+        if (ncols == 4) sscanf(line, "%63s %lf %lf %lf", type, &x, &y, &z);
+        else if (ncols == 5) sscanf(line, "%63s %lf %lf %lf %lf", type, &x, &y, &z, &q);
+        else if (ncols == 6) sscanf(line, "%63s %lf %lf %lf %lf %d", type, &x, &y, &z, &q, &fx);
+        else fail(MAFM_E_PARSE, "Invalid number of columns in the xyz file.");
+        if (atom_i >= in.n_atoms)
+            fail(MAFM_E_PARSE, "More atoms in the xyz file than given on its first line.");
+        in.types[atom_i] = type;
+        in.pos[3 * atom_i] = x;
+        in.pos[3 * atom_i + 1] = y;
+        in.pos[3 * atom_i + 2] = z;
+        in.charges[atom_i] = q;
+        in.fixed[atom_i] = in.flexible ? fx : 1;
+        atom_i++;
+    }
+    double check = 0;
+    for (int i = 0; i < in.n_atoms; ++i) check += in.charges[i] * in.charges[i];
+    if (fabs(check) < kTolerance) {
+        in.xyz_charges = false;
+        warn(in, "The RMSQ-error for the charges read from the XYZ-file is zero.\n"
+                 "+-     Charges will be read from the parameter file.\n"
+                 "+-     If you want zero charge, set the charge in the parameter file to zero.\n"
+                 "+-");
+    } else {
+        in.xyz_charges = true;
+    }
+}
+
+// readFlexibleParameters, parse.cpp:699-782 (parsed for completeness of the
+// boundary; flexible scans are not run on the GPU).
+void read_flexible(mafm_input& in, FILE* fp) {
+    char line[kLine], keyword[128] = "", dump[128];
+    bool b = false, a = false, d = false, s = false;
+    while (fgets(line, kLine, fp)) {
+        if (is_comment(line)) continue;
+        sscanf(line, "%127s", keyword);
+        if (!strcmp(keyword, "bond")) {
+            if (b) warn(in, "Parameters for harmonic bond defined multiple times!");
+            sscanf(line, "%127s %lf", dump, &in.bond_k);
+            b = true;
+        }
+        if (!strcmp(keyword, "angle")) {
+            if (a) warn(in, "Parameters for harmonic angle defined multiple times!");
+            sscanf(line, "%127s %lf", dump, &in.angle_k);
+            a = true;
+        }
+        if (!strcmp(keyword, "dihedral")) {
+            if (d) warn(in, "Parameters for harmonic dihedral defined multiple times!");
+            sscanf(line, "%127s %lf", dump, &in.dihedral_k);
+            d = true;
+        }
+        if (!strcmp(keyword, "substrate")) {
+            if (s) warn(in, "Parameters for substrate support defined multiple times!");
+            sscanf(line, "%127s %lf %lf %lf %lf %lf", dump, &in.sub_eps, &in.sub_sig,
+                   &in.sub_lambda, &in.sub_rc, &in.sub_k);
+            s = true;
+        }
+    }
+    if (!b) fail(MAFM_E_PARSE, "No harmonic bond parameters found in parameter file!");
+    if (!a) fail(MAFM_E_PARSE, "No harmonic angle parameters found in parameter file!");
+    if (!d) fail(MAFM_E_PARSE, "No harmonic dihedral parameters found in parameter file!");
+    if (!s) fail(MAFM_E_PARSE, "No harmonic substrate support parameters found in parameter file!");
+}
+
+// readParameterFile, parse.cpp:588-697.
+void read_params(mafm_input& in) {
+    FILE* fp = fopen(in.paramfile.c_str(), "r");
+    if (!fp) fail(MAFM_E_IO, "No parameter file %s found!", in.paramfile.c_str());
+    struct Closer { FILE* f; ~Closer() { fclose(f); } } closer{fp};
+    char line[kLine], keyword[128] = "", dump[kLine], atom[64] = "", a1[64] = "", a2[64] = "",
+         style[128] = "";
+    double eps = 0, sig = 0, mass = 0, q = 0, de = 0, alpha = 0, re = 0;
+    bool hcheck = false;
+    while (fgets(line, kLine, fp)) {
+        if (is_comment(line)) continue;
+        sscanf(line, "%127s", keyword);
+        if (!strcmp(keyword, "atom")) {
+            sscanf(line, "%127s %63s %lf %lf %lf %lf", dump, atom, &eps, &sig, &mass, &q);
+            if (in.ap.count(atom)) warn(in, "Parameters for atom type %s defined multiple times.", atom);
+            AtomParams& p = in.ap[atom];
+            p.eps = eps;
+            p.sig = sig;
+            p.q = q;
+            p.mass = mass;
+            if (in.dummyatom == atom) in.charges[0] = q;
+            if (in.tipatom == atom) in.charges[1] = q;
+        } else if (!strcmp(keyword, "harm")) {
+            if (hcheck) fail(MAFM_E_PARSE, "Parameters for harmonic spring can only be specified once!");
+            sscanf(line, "%127s %lf %lf", dump, &in.harm_k, &in.harm_r0);
+            hcheck = true;
+        } else if (!strcmp(keyword, "pair_ovwrt")) {
+            sscanf(line, "%127s %63s %63s %127s", dump, a1, a2, style);
+            int ncols = count_columns(line);
+            if (!strcmp(style, "lj")) {
+                if (ncols != 4 + 2) fail(MAFM_E_PARSE, "Only two parameters (eps, sig) allowed for LJ");
+                sscanf(line, "%127s %127s %127s %127s %lf %lf", dump, dump, dump, dump, &eps, &sig);
+                Overwrite o;
+                o.a = a1; o.b = a2; o.eps = eps; o.sig = sig; o.morse = false;
+                in.ow.push_back(o);
+            } else if (!strcmp(style, "morse")) {
+                if (ncols != 4 + 3) fail(MAFM_E_PARSE, "Only three parameters (De, a, re) allowed for Morse");
+                sscanf(line, "%127s %127s %127s %127s %lf %lf %lf", dump, dump, dump, dump, &de, &alpha, &re);
+                Overwrite o;
+                o.a = a1; o.b = a2; o.de = de; o.alpha = alpha; o.re = re; o.morse = true;
+                in.ow.push_back(o);
+            } else {
+                fail(MAFM_E_PARSE, "Unknown pair style overwrite '%s'", style);
+            }
+        }
+    }
+    if (!hcheck) fail(MAFM_E_PARSE, "No harmonic spring parameters found in parameter file!");
+    if (in.flexible) {
+        rewind(fp);
+        read_flexible(in, fp);
+    }
+}
+
+// Gaussian cube, CubeReader::readMetadata + readVolumetricData (cube_io.cpp:10-139).
+struct Cube {
+    int n[3] = {0, 0, 0};
+    double voxel[3][3] = {{0}};   // voxel[i] = vector i (Angstrom)
+    double origin[3] = {0, 0, 0};
+    std::vector<double> values;
+};
+
+Cube read_cube(const std::string& path, bool with_values) {
+    FILE* fp = fopen(path.c_str(), "r");
+    if (!fp) fail(MAFM_E_IO, "Could not read metadata from the cube file. Check the format of the file.");
+    std::string text;
+    {
+        char buf[1 << 16];
+        size_t k;
+        while ((k = fread(buf, 1, sizeof buf, fp)) > 0) text.append(buf, k);
+        fclose(fp);
+    }
+    const char* p = text.c_str();
+    for (int l = 0; l < 2; ++l) {
+        const char* nl = strchr(p, '\n');
+        if (!nl) fail(MAFM_E_PARSE, "Could not read metadata from the cube file. Check the format of the file.");
+        p = nl + 1;
+    }
+    auto next_d = [&](double& v) {
+        char* e;
+        v = strtod(p, &e);
+        if (e == p) fail(MAFM_E_PARSE, "Could not read metadata from the cube file. Check the format of the file.");
+        p = e;
+    };
+    auto next_i = [&](int& v) {
+        char* e;
+        long x = strtol(p, &e, 10);
+        if (e == p) fail(MAFM_E_PARSE, "Could not read metadata from the cube file. Check the format of the file.");
+        v = (int)x;
+        p = e;
+    };
+    Cube c;
+    int natoms;
+    next_i(natoms);
+    for (int d = 0; d < 3; ++d) next_d(c.origin[d]);
+    for (int v = 0; v < 3; ++v) {
+        next_i(c.n[v]);
+        for (int d = 0; d < 3; ++d) next_d(c.voxel[v][d]);
+    }
+    if (c.n[0] < 0) {
+        for (int v = 0; v < 3; ++v) c.n[v] = -c.n[v];
+    } else {
+        for (int v = 0; v < 3; ++v)
+            for (int d = 0; d < 3; ++d) c.voxel[v][d] *= kBohr;
+        for (int d = 0; d < 3; ++d) c.origin[d] *= kBohr;
+    }
+    if (natoms < 0 || c.n[0] <= 0 || c.n[1] <= 0 || c.n[2] <= 0)
+        fail(MAFM_E_PARSE, "Could not read metadata from the cube file. Check the format of the file.");
+    for (int a = 0; a < natoms; ++a) {
+        int z;
+        double t;
+        next_i(z);
+        for (int k = 0; k < 4; ++k) next_d(t);
+    }
+    if (with_values) {
+        const size_t total = (size_t)c.n[0] * c.n[1] * c.n[2];
+        c.values.resize(total);
+        for (size_t i = 0; i < total; ++i) {
+            char* e;
+            double v = strtod(p, &e);
+            if (e == p)
+                fail(MAFM_E_PARSE, "Could not read the volumetric data from the cube file. Check the format of the file.");
+            c.values[i] = v;
+            p = e;
+        }
+    }
+    return c;
+}
+
+// System::rotateCoordAxes, system.cpp:68-90 (positions only).
+void rotate_positions(mafm_input& in, const char* seq) {
+    for (int a = 0; a < in.n_atoms; ++a) {
+        double x = in.pos[3 * a], y = in.pos[3 * a + 1], z = in.pos[3 * a + 2];
+        if (!strcmp(seq, "ZXY")) {
+            in.pos[3 * a] = z; in.pos[3 * a + 1] = x; in.pos[3 * a + 2] = y;
+        } else {
+            in.pos[3 * a] = y; in.pos[3 * a + 1] = z; in.pos[3 * a + 2] = x;
+        }
+    }
+}
+
+// LJ or Morse parameters of a pair, Simulation::addVDWInteraction (simulation.cpp:238-267).
+mafm_pair resolve_vdw(const mafm_input& in, const std::string& t1, const std::string& t2) {
+    mafm_pair p{};
+    for (const Overwrite& o : in.ow) {
+        if (multiset_eq(o.a, o.b, t1, t2)) {
+            if (o.morse) {
+                p.kind = MAFM_PAIR_MORSE;
+                p.p[0] = o.de; p.p[1] = o.alpha; p.p[2] = o.re;
+            } else {
+                p.kind = MAFM_PAIR_LJ;
+                p.p[0] = 4 * o.eps * pow(o.sig, 6);
+                p.p[1] = 4 * o.eps * pow(o.sig, 12);
+            }
+            return p;
+        }
+    }
+    auto i1 = in.ap.find(t1), i2 = in.ap.find(t2);
+    if (i1 == in.ap.end()) fail(MAFM_E_PARSE, "Parameters for atom type %s not found in parameter file!", t1.c_str());
+    if (i2 == in.ap.end()) fail(MAFM_E_PARSE, "Parameters for atom type %s not found in parameter file!", t2.c_str());
+    double m_eps = sqrt(i1->second.eps * i2->second.eps);
+    double m_sig = (i1->second.sig + i2->second.sig) / 2;
+    p.kind = MAFM_PAIR_LJ;
+    p.p[0] = 4 * m_eps * pow(m_sig, 6);
+    p.p[1] = 4 * m_eps * pow(m_sig, 12);
+    return p;
+}
+
+// Charge of atom i for a Coulomb term, Simulation::addCoulombInteraction (simulation.cpp:269-289).
+double coulomb_charge(const mafm_input& in, int i) {
+    if (in.xyz_charges) return in.charges[i];
+    auto it = in.ap.find(in.types[i]);
+    if (it == in.ap.end())
+        fail(MAFM_E_PARSE, "Parameters for atom type %s not found in parameter file!", in.types[i].c_str());
+    return it->second.q;
+}
+
+// Simulation::initialize and the parameter part of buildInteractions.
+void prepare(mafm_input& in) {
+    in.np[0] = (int)(floor(in.area[0] / in.dx) + 1);
+    in.np[1] = (int)(floor(in.area[1] / in.dy) + 1);
+    in.np[2] = (int)(floor((in.zhigh - in.zlow) / in.dz) + 1);
+    if (in.normal == NORMAL_X) rotate_positions(in, "YZX");
+    else if (in.normal == NORMAL_Y) rotate_positions(in, "ZXY");
+    if (in.vdw_pbc) {
+        double cv[3][3];
+        if (in.use_external_potential) {
+            Cube c = read_cube(in.e_potential_file, false);
+            for (int v = 0; v < 3; ++v)
+                for (int d = 0; d < 3; ++d) cv[v][d] = c.n[v] * c.voxel[v][d];
+        } else {
+            for (int d = 0; d < 3; ++d) {
+                cv[0][d] = in.cell_a[d]; cv[1][d] = in.cell_b[d]; cv[2][d] = in.cell_c[d];
+            }
+        }
+        for (int v = 0; v < 3; ++v)
+            for (int d = 0; d < 3; ++d) in.cell.v[d][v] = cv[v][d];
+        in.tip_pbc = true;
+    }
+    // System::centerMolecule (system.cpp:119-136)
+    double avgx = 0.0, avgy = 0.0;
+    for (int i = 2; i < in.n_atoms; ++i) {
+        avgx += in.pos[3 * i];
+        avgy += in.pos[3 * i + 1];
+    }
+    avgx /= in.n_atoms - 2;
+    avgy /= in.n_atoms - 2;
+    double ddx = in.center[0] - avgx, ddy = in.center[1] - avgy;
+    for (int i = 2; i < in.n_atoms; ++i) {
+        in.pos[3 * i] += ddx;
+        in.pos[3 * i + 1] += ddy;
+    }
+    in.offset[0] = ddx;
+    in.offset[1] = ddy;
+    // System::setMoleculeZ (system.cpp:103-116)
+    double min_z = 10e10;
+    for (int i = 2; i < in.n_atoms; ++i)
+        if (in.pos[3 * i + 2] < min_z && in.types[i] != "H") min_z = in.pos[3 * i + 2];
+    for (int i = 2; i < in.n_atoms; ++i) in.pos[3 * i + 2] -= min_z;
+    in.offset[2] = -min_z;
+    // Simulation::calculateTipDummyDistance (simulation.cpp:218-225)
+    auto dm = in.ap.find(in.types[0]), tp = in.ap.find(in.types[1]);
+    if (dm == in.ap.end()) fail(MAFM_E_PARSE, "Parameters for atom type %s not found in parameter file!", in.types[0].c_str());
+    if (tp == in.ap.end()) fail(MAFM_E_PARSE, "Parameters for atom type %s not found in parameter file!", in.types[1].c_str());
+    in.tip_dummy_d = (dm->second.sig + tp->second.sig) / 2 * kSixthRoot2;
+
+    // Surface atoms: type table in order of first appearance, tip pair per type.
+    std::map<std::string, int> index;
+    const int ns = in.n_atoms - 2;
+    in.d_pos.assign(3 * (size_t)ns, 0.0);
+    in.d_charge.assign(ns, 0.0);
+    in.d_type.assign(ns, 0);
+    in.type_names.clear();
+    in.d_pairs.clear();
+    for (int i = 2; i < in.n_atoms; ++i) {
+        auto it = index.find(in.types[i]);
+        int t;
+        if (it == index.end()) {
+            t = (int)in.type_names.size();
+            index[in.types[i]] = t;
+            in.type_names.push_back(in.types[i]);
+            in.d_pairs.push_back(resolve_vdw(in, in.types[1], in.types[i]));
+        } else {
+            t = it->second;
+        }
+        in.d_type[i - 2] = t;
+        for (int d = 0; d < 3; ++d) in.d_pos[3 * (i - 2) + d] = in.pos[3 * i + d];
+    }
+    // Charges.  Whether read from the xyz file or looked up by type, the tip's
+    // and the dummy's charges are System::charges_[1] and [0]: the parameter
+    // file's line for their type sets both (parse.cpp:626-631).  The lookups
+    // still run where the reference runs them, for its error messages.
+    in.tip_q_eff = in.charges[1];
+    in.dummy_q_eff = in.charges[0];
+    if (in.coulomb && !in.vdw_pbc) {
+        (void)coulomb_charge(in, 1);
+        for (int i = 2; i < in.n_atoms; ++i) in.d_charge[i - 2] = coulomb_charge(in, i);
+    }
+    in.dummy_pair = resolve_vdw(in, in.types[0], in.types[1]);
+    if (in.tip_dummy_coulomb) {
+        (void)coulomb_charge(in, 0);
+        (void)coulomb_charge(in, 1);
+    }
+    if (in.use_external_potential) {
+        // The field's tip charge is System::charges_[1] as well (simulation.cpp:415).
+        Cube c = read_cube(in.e_potential_file, true);
+        double scale = in.units == MAFM_UNITS_EV ? -kHartreeEV
+                     : in.units == MAFM_UNITS_KJ ? -kHartreeKJ : -kHartreeKcal;
+        for (double& v : c.values) v *= scale;
+        M3 basis;
+        for (int v = 0; v < 3; ++v)
+            for (int d = 0; d < 3; ++d) basis.v[d][v] = c.voxel[v][d];
+        double origin[3] = {c.origin[0], c.origin[1], c.origin[2]};
+        int n[3] = {c.n[0], c.n[1], c.n[2]};
+        if (in.normal == NORMAL_X) {
+            // The reference asks DataGrid::rotateCoordAxes for "ZYX", which it
+            // rejects (simulation.cpp:358-359, data_grid.cpp:92-94).
+            fail(MAFM_E_PARSE, "The coordinate sequence for rotateCoordAxes must be either ZXY or YZX.");
+        } else if (in.normal == NORMAL_Y) {
+            // DataGrid::rotateCoordAxes("ZXY"), data_grid.cpp:40-69
+            int nn[3] = {n[2], n[0], n[1]};
+            M3 S;
+            S.v[2][0] = 1; S.v[0][1] = 1; S.v[1][2] = 1;
+            basis = S.transpose().mul(basis.mul(S));
+            double no[3] = {origin[2], origin[0], origin[1]};
+            std::vector<double> nv(c.values.size());
+            for (int ix = 0; ix < nn[0]; ix++)
+                for (int iy = 0; iy < nn[1]; iy++)
+                    for (int iz = 0; iz < nn[2]; iz++)
+                        nv[((size_t)ix * nn[1] + iy) * nn[2] + iz] =
+                            c.values[((size_t)iy * n[1] + iz) * n[2] + ix];
+            c.values.swap(nv);
+            for (int d = 0; d < 3; ++d) { n[d] = nn[d]; origin[d] = no[d]; }
+        }
+        for (int d = 0; d < 3; ++d) in.epot_origin[d] = origin[d] + in.offset[d];
+        for (int d = 0; d < 3; ++d) in.epot_n[d] = n[d];
+        in.epot_basis = basis;
+        in.epot.swap(c.values);
+    }
+}
+
+}  // namespace
+
+// ----- output (writeOutput, simulation.cpp:145-199) -------------------------
+
+namespace {
+
+void write_rows(const mafm_input& in, const mafm_point* pts, int k, FILE* f) {
+    const int nx = in.np[0], ny = in.np[1], nz = in.np[2];
+    // Dummy z after k calls of lowerTip (system.hpp:51-54).
+    double dz_acc = in.zhigh;
+    for (int s = 0; s < k; ++s) dz_acc -= in.dz;
+    const bool wrap = in.tip_pbc && !in.rigidgrid;
+    const M3 inv = in.cell.inverse();
+    std::string buf;
+    buf.reserve((size_t)ny * 120);
+    char row[512];
+    for (int i = 0; i < nx; ++i) {
+        buf.clear();
+        for (int j = 0; j < ny; ++j) {
+            const mafm_point& p = pts[((size_t)i * ny + j) * nz + k];
+            const double x = i * in.dx, y = j * in.dy;
+            double dxy[2] = {x, y};
+            if (wrap) {
+                // System::setDummyXY with periodic boundaries (system.cpp:139-162)
+                double t[3] = {x - in.offset[0], y - in.offset[1], 0 - in.offset[2]};
+                double cn[3];
+                for (int r = 0; r < 3; ++r)
+                    cn[r] = inv.v[r][0] * t[0] + inv.v[r][1] * t[1] + inv.v[r][2] * t[2];
+                cn[0] -= floor(cn[0]);
+                cn[1] -= floor(cn[1]);
+                for (int r = 0; r < 2; ++r)
+                    dxy[r] = in.cell.v[r][0] * cn[0] + in.cell.v[r][1] * cn[1] +
+                             in.cell.v[r][2] * cn[2] + in.offset[r];
+            }
+            const double rx = p.tip[0] - dxy[0], ry = p.tip[1] - dxy[1], rz = p.tip[2] - dz_acc;
+            const double r = sqrt(rx * rx + ry * ry + rz * rz);
+            const double angle = atan2(sqrt(rx * rx + ry * ry), rz) * (180.0 / kPi);
+            int len = snprintf(row, sizeof row,
+                               "%d %d %d %6.3f %6.3f %6.3f %8.4f %8.4f %8.4f %6.3f %6.3f %6.3f "
+                               "%6.3f %8.4f %8.4f %d\n",
+                               k, i, j, x, y, dz_acc, p.force[0], p.force[1], p.force[2], rx, ry,
+                               rz, r, angle, p.energy, p.steps);
+            buf.append(row, (size_t)len);
+        }
+        fwrite(buf.data(), 1, buf.size(), f);
+    }
+}
+
+}  // namespace
+}  // namespace mafm
+
+// ----- C ABI ------------------------------------------------------------------
+
+extern "C" {
+
+const char* mafm_last_error(void) { return mafm::g_last_error.c_str(); }
+
+int mafm_abi_version(void) { return MAFM_ABI_VERSION; }
+
+int mafm_input_load(const char* input_file, int verbose, mafm_input** out) {
+    return mafm::guarded([&] {
+        if (!input_file || !out) mafm::fail(MAFM_E_INVALID, "null argument");
+        *out = nullptr;
+        auto* in = new mafm_input();
+        try {
+            in->verbose = verbose != 0;
+            in->inputfile = input_file;
+            size_t split = in->inputfile.rfind('/');
+            if (split != std::string::npos) in->inputfolder = in->inputfile.substr(0, split + 1);
+            mafm::read_input(*in);
+            mafm::read_xyz(*in);
+            mafm::read_params(*in);
+            mafm::prepare(*in);
+        } catch (...) {
+            delete in;
+            throw;
+        }
+        *out = in;
+    });
+}
+
+int mafm_input_desc(const mafm_input* in, mafm_scan_desc* d) {
+    return mafm::guarded([&] {
+        if (!in || !d) mafm::fail(MAFM_E_INVALID, "null argument");
+        if (in->flexible)
+            mafm::fail(MAFM_E_UNSUPPORTED, "flexible molecules are not run by this library");
+        *d = mafm_scan_desc{};
+        d->n_atoms = in->n_atoms - 2;
+        d->n_types = (int32_t)in->type_names.size();
+        d->pos = in->d_pos.data();
+        d->charge = in->d_charge.data();
+        d->type = in->d_type.data();
+        d->tip_pair = in->d_pairs.data();
+        d->dummy_pair = in->dummy_pair;
+        d->tip_charge = in->tip_q_eff;
+        d->dummy_charge = in->dummy_q_eff;
+        d->qbase = in->qbase;
+        d->coulomb = in->coulomb && !in->vdw_pbc;
+        d->tip_dummy_coulomb = in->tip_dummy_coulomb;
+        d->harm_k = in->harm_k;
+        d->harm_r0 = in->harm_r0;
+        d->tip_dummy_d = in->tip_dummy_d;
+        d->vdw_pbc = in->vdw_pbc;
+        d->tip_pbc = in->tip_pbc;
+        for (int r = 0; r < 3; ++r)
+            for (int c = 0; c < 3; ++c) d->cell[3 * r + c] = in->cell.v[r][c];
+        for (int k = 0; k < 3; ++k) d->offset[k] = in->offset[k];
+        d->nx = in->np[0];
+        d->ny = in->np[1];
+        d->nz = in->np[2];
+        d->dx = in->dx;
+        d->dy = in->dy;
+        d->dz = in->dz;
+        d->zhigh = in->zhigh;
+        d->zlow = in->zlow;
+        d->area[0] = in->area[0];
+        d->area[1] = in->area[1];
+        d->minimiser = in->minimiser;
+        d->integrator = in->integrator;
+        d->minterm = in->minterm;
+        d->maxsteps = in->maxsteps;
+        d->etol = in->etol;
+        d->ftol = in->ftol;
+        d->dt = in->dt;
+        d->rigidgrid = in->rigidgrid;
+        d->use_external_potential = in->use_external_potential;
+        if (in->use_external_potential) {
+            d->epot = in->epot.data();
+            for (int k = 0; k < 3; ++k) d->epot_n[k] = in->epot_n[k];
+            for (int r = 0; r < 3; ++r)
+                for (int c = 0; c < 3; ++c) d->epot_basis[3 * r + c] = in->epot_basis.v[r][c];
+            for (int k = 0; k < 3; ++k) d->epot_origin[k] = in->epot_origin[k];
+        }
+    });
+}
+
+int mafm_input_output_opts(const mafm_input* in, int32_t* gzip, int32_t* statistics,
+                           int32_t* bufsize) {
+    return mafm::guarded([&] {
+        if (!in) mafm::fail(MAFM_E_INVALID, "null argument");
+        if (gzip) *gzip = in->gzip;
+        if (statistics) *statistics = in->statistics;
+        if (bufsize) *bufsize = in->bufsize;
+    });
+}
+
+int mafm_input_free(mafm_input* in) {
+    delete in;
+    return MAFM_OK;
+}
+
+int mafm_write_output(const mafm_input* in, const mafm_point* pts, const char* folder,
+                      int32_t gzip) {
+    return mafm::guarded([&] {
+        if (!in || !pts || !folder) mafm::fail(MAFM_E_INVALID, "null argument");
+        const int nz = in->np[2];
+        std::vector<FILE*> files(nz, nullptr);
+        char name[1024];
+        for (int k = 0; k < nz; ++k) {
+            const double z = in->zhigh - k * in->dz;
+            if (gzip) {
+                snprintf(name, sizeof name, "gzip -6 > %sscan-%06.3f.dat.gz", folder, z);
+                files[k] = popen(name, "w");
+            } else {
+                snprintf(name, sizeof name, "%sscan-%06.3f.dat", folder, z);
+                files[k] = fopen(name, "w");
+            }
+            if (!files[k]) mafm::fail(MAFM_E_IO, "cannot open %s", name);
+        }
+        // One z-file per task; files are independent, so they are written in parallel.
+#pragma omp parallel for schedule(dynamic, 1)
+        for (int k = 0; k < nz; ++k) mafm::write_rows(*in, pts, k, files[k]);
+        for (int k = 0; k < nz; ++k) {
+            if (gzip) pclose(files[k]);
+            else fclose(files[k]);
+        }
+    });
+}
+
+int mafm_write_statistics(const mafm_input* in, const char* folder, uint64_t total_steps,
+                          double wall_s, double total_s) {
+    return mafm::guarded([&] {
+        if (!in || !folder) mafm::fail(MAFM_E_INVALID, "null argument");
+        std::string path = std::string(folder) + "statistics.txt";
+        FILE* fp = fopen(path.c_str(), "w");
+        if (!fp) mafm::fail(MAFM_E_IO, "cannot open %s", path.c_str());
+        const int n_points = in->np[0] * in->np[1] * in->np[2];
+        fprintf(fp, "Simulation run finished\n");
+        fprintf(fp, "Statistics:\n");
+        fprintf(fp, "    Computed %d tip positions\n", n_points);
+        fprintf(fp, "    Needed %ld minimization steps in total\n", (long)total_steps);
+        fprintf(fp, "    Which means approximately %.2f minimization steps per tip position\n",
+                ((double)total_steps / n_points));
+        fprintf(fp, "    The simulation wall time is %.2f seconds\n", wall_s);
+        fprintf(fp, "    The entire simulation took %.2f seconds\n", total_s);
+        fclose(fp);
+    });
+}
+
+}  // extern "C"

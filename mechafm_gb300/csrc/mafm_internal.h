@@ -1,0 +1,155 @@
+// mafm_internal.h — structures shared by the host library and the kernels.
+//
+// Device data layout (HBM):
+//   atoms64  AtomRec64[n]   64 B per tip–atom term, in the reference's
+//                           interaction order (simulation.cpp:297-320): for
+//                           vdw_pbc the 3x3 images are the outer loop and the
+//                           atoms the inner loop; positions already carry the
+//                           image shift (interactions.cpp:16,30).
+//   atoms32  AtomRec32[n]   32 B per term: float4 {x,y,z,qq} + float4 {p0,p1,p2,kind}
+//   grid64   Node64[n]     rigid force grid {Fx,Fy,Fz,E}, index (i*ny+j)*nz+k
+//   grid32   float4[n]      same in FP32
+//   es64/es32               external-field grid, same layout
+#pragma once
+
+#include <cstdint>
+#include <new>
+#include <stdexcept>
+#include <string>
+#include <cuda_runtime.h>
+
+#include "mafm.h"
+
+namespace mafm {
+
+// Host-side failure carried to the C ABI boundary, where it becomes a status
+// code plus mafm_last_error() text.  Never crosses extern "C".
+struct Failure {
+    int code;
+    std::string msg;
+};
+[[noreturn]] void fail(int code, const char* fmt, ...);
+void set_last_error(const std::string& msg);
+
+template <class F>
+int guarded(F&& f) {
+    try {
+        f();
+        return MAFM_OK;
+    } catch (const Failure& e) {
+        set_last_error(e.msg);
+        return e.code;
+    } catch (const std::bad_alloc&) {
+        set_last_error("host allocation failed");
+        return MAFM_E_NOMEM;
+    } catch (const std::exception& e) {
+        set_last_error(e.what());
+        return MAFM_E_INVALID;
+    }
+}
+
+inline void cuda_check(cudaError_t e, const char* what) {
+    if (e != cudaSuccess) fail(MAFM_E_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+// Device error bits (mafm_run_stats.error_word, upper half; lower bits are MAFM_PT_*).
+enum : uint32_t {
+    ERR_GRID_INDEX = 1u << 16,   // corner outside a non-periodic grid (force_grid.cpp:236-240)
+    ERR_STAGE_TIMEOUT = 1u << 17 // bounded wait on the atom staging barrier expired
+};
+
+struct __align__(16) AtomRec64 {
+    double x, y, z, qq;    // image position, Coulomb prefactor qbase*q_tip*q_atom
+    double p0, p1, p2;     // LJ: es6, es12, - ; Morse: De, a, re
+    int32_t kind;          // MAFM_PAIR_*
+    int32_t coul;          // 1 if a Coulomb term follows the vdW term
+};
+
+// One FP64 grid node {Fx, Fy, Fz, E}.
+struct __align__(32) Node64 {
+    double x, y, z, w;
+};
+
+struct __align__(16) AtomRec32 {
+    float4 a;              // x, y, z, qq
+    float4 b;              // p0, p1, p2, kind (int bits)
+};
+
+// A trilinear force grid (ForceGrid, force_grid.hpp:15-51).
+struct GridView {
+    const Node64* g64;
+    const float4* g32;
+    int n[3];
+    int periodic;
+    int orthogonal;
+    int pad;
+    double basis[9];       // row-major, columns are the node steps
+    double inv[9];         // inverse of basis (Matrix3::inverse)
+    double origin[3];
+};
+
+// Everything a relax / build / sample kernel needs for one scan.
+struct ScanParams {
+    // tip–atom terms
+    int n_terms;
+    int n_terms_direct;    // terms evaluated per force call (0 in rigid-grid mode)
+    const AtomRec64* atoms64;
+    const AtomRec32* atoms32;
+    // tip–surface source of the relax: 0 pairs, 1 pairs + external field, 2 rigid grid
+    int ts_mode;
+    int pad0;
+    GridView grid;         // rigid grid (ts_mode 2)
+    GridView es;           // external field (ts_mode 1, and grid build)
+    // tip–dummy coupling (buildTipDummyInteractions, simulation.cpp:503-515)
+    int td_kind;
+    int td_coul;
+    double td_p[3];
+    double td_qq;
+    double harm_k, harm_r0;
+    double tip_dummy_d;
+    // pixel grid and z descent
+    int nx, ny, nz;
+    int tip_pbc;
+    double dx, dy, dz, zhigh;
+    double cell[9], cell_inv[9], offset[3];
+    // minimiser
+    int minimiser, integrator, minterm, maxsteps;
+    double etol, ftol, dt;
+};
+
+// Counters the relax kernels update (device memory owned by the scan).
+struct RunCounters {
+    unsigned long long next_work;     // persistent work queue head
+    unsigned long long total_steps;
+    unsigned long long force_evals;
+    unsigned long long pair_evals;
+    unsigned int error_word;
+    unsigned int pad;
+};
+
+// Launchers implemented in relax64.cu / relax32.cu.
+cudaError_t launch_relax64(const ScanParams& p, mafm_point* out, RunCounters* ctr,
+                           int col_begin, int col_end, int block, cudaStream_t s);
+cudaError_t launch_sample64(const ScanParams& p, int what, const double* pts, int64_t n,
+                            double* out, cudaStream_t s);
+cudaError_t launch_grid_build64(const ScanParams& p, const GridView& g, Node64* out,
+                                cudaStream_t s);
+
+// One entry of a multi-scan work list for the FP32 persistent kernel.
+struct BatchScan {
+    ScanParams p;
+    mafm_point* out;
+    long long tile_begin;     // first global tile index of this scan
+    int col_begin, col_end;
+};
+
+cudaError_t launch_relax32(const BatchScan* scans_dev, int n_scans, long long n_tiles,
+                           int cols_per_tile, int lanes, int block, int max_terms,
+                           RunCounters* ctr, cudaStream_t s);
+cudaError_t launch_sample32(const ScanParams& p, int what, const double* pts, int64_t n,
+                            double* out, cudaStream_t s);
+cudaError_t launch_grid_build32(const ScanParams& p, const GridView& g, float4* out,
+                                cudaStream_t s);
+int relax32_smem_terms_limit(int block);
+
+}  // namespace mafm

@@ -1,0 +1,168 @@
+"""Python face of the libmafm C ABI (include/mafm.h).
+
+Mirrors the reference's process flow (src/mechafm.cpp:209-233): load the input
+files (readInputFile / readXYZFile / readParameterFile), prepare the System,
+relax every pixel column, write the scan files.  Every call goes through the
+C ABI; there is no Python or CPU compute path, and a missing libmafm.so is an
+error.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import _abi
+from ._abi import check, lib, ptr
+
+
+class Input:
+    """Parsed input files plus the prepared System (opaque mafm_input)."""
+
+    def __init__(self, input_file: str, verbose: bool = False):
+        h = C.c_void_p()
+        check(lib().mafm_input_load(os.fsencode(input_file), int(verbose), C.byref(h)))
+        self._h = h
+        self.path = input_file
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().mafm_input_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self):
+        return self._h
+
+    def desc(self) -> "Desc":
+        d = _abi.ScanDesc()
+        check(lib().mafm_input_desc(self._h, C.byref(d)))
+        return Desc(d, keep=self)
+
+    def output_opts(self):
+        g, s, b = C.c_int32(), C.c_int32(), C.c_int32()
+        check(lib().mafm_input_output_opts(self._h, C.byref(g), C.byref(s), C.byref(b)))
+        return {"gzip": bool(g.value), "statistics": bool(s.value), "bufsize": b.value}
+
+    def write_output(self, points: np.ndarray, folder: str, gzip: bool | None = None):
+        if gzip is None:
+            gzip = self.output_opts()["gzip"]
+        if folder and not folder.endswith("/"):
+            folder += "/"
+        points = np.ascontiguousarray(points, dtype=_abi.POINT_DTYPE)
+        check(lib().mafm_write_output(self._h, ptr(points), os.fsencode(folder), int(gzip)))
+
+
+class Desc:
+    """A mafm_scan_desc plus whatever owns the memory its pointers refer to."""
+
+    def __init__(self, c: _abi.ScanDesc, keep=None):
+        self.c = c
+        self._keep = keep
+
+    @property
+    def n_columns(self) -> int:
+        return self.c.nx * self.c.ny
+
+    @property
+    def n_points(self) -> int:
+        return self.c.nx * self.c.ny * self.c.nz
+
+    @property
+    def shape(self):
+        return (self.c.nx, self.c.ny, self.c.nz)
+
+    def atoms(self) -> dict:
+        n = self.c.n_atoms
+        return {
+            "pos": np.ctypeslib.as_array(self.c.pos, shape=(n * 3,)).reshape(n, 3).copy(),
+            "charge": np.ctypeslib.as_array(self.c.charge, shape=(n,)).copy(),
+            "type": np.ctypeslib.as_array(self.c.type, shape=(n,)).copy(),
+        }
+
+
+def run_opts(precision=_abi.FP64, lanes=0, block=0, tile=0, col_begin=0, col_end=0):
+    return _abi.RunOpts(precision, lanes, block, tile, col_begin, col_end)
+
+
+class Scan:
+    """A device-resident scan (mafm_scan)."""
+
+    def __init__(self, desc: Desc, device: int = -1):
+        h = C.c_void_p()
+        check(lib().mafm_scan_create(device, C.byref(desc.c), C.byref(h)))
+        self._h = h
+        self.desc = desc
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().mafm_scan_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self):
+        return self._h
+
+    def run(self, precision=_abi.FP64, lanes=0, block=0, tile=0, col_begin=0, col_end=0,
+            out: np.ndarray | None = None, stream=None):
+        """Relax the scan; returns (points, stats) with points in host memory."""
+        n_cols = (col_end - col_begin) if col_end else self.desc.n_columns
+        if out is None:
+            out = np.zeros(n_cols * self.desc.c.nz, dtype=_abi.POINT_DTYPE)
+        stats = _abi.RunStats()
+        o = run_opts(precision, lanes, block, tile, col_begin, col_end)
+        check(lib().mafm_run(self._h, C.byref(o), ptr(out), C.byref(stats), stream))
+        return out, stats
+
+    def run_device(self, out_ptr: int, precision=_abi.FP32C, lanes=0, block=0, tile=0,
+                   stream=None, stats: bool = False):
+        """Relax into device memory at out_ptr (no copy back).  stats=True synchronises."""
+        st = _abi.RunStats() if stats else None
+        o = run_opts(precision, lanes, block, tile)
+        check(lib().mafm_run(self._h, C.byref(o), C.c_void_p(out_ptr),
+                             C.byref(st) if st is not None else None, stream))
+        return st
+
+    def sample(self, pts: np.ndarray, precision=_abi.FP64, what: int = 0) -> np.ndarray:
+        pts = np.ascontiguousarray(pts, dtype=np.float64).reshape(-1, 3)
+        out = np.zeros((len(pts), 4))
+        check(lib().mafm_scan_sample(self._h, precision, what, ptr(pts), len(pts), ptr(out)))
+        return out
+
+    def grid_info(self, what: int = 0):
+        n = (C.c_int32 * 3)()
+        b = (C.c_double * 9)()
+        o = (C.c_double * 3)()
+        check(lib().mafm_scan_grid_info(self._h, what, n, b, o))
+        return tuple(n), np.array(b[:]).reshape(3, 3), np.array(o[:])
+
+    def grid(self, what: int = 0) -> np.ndarray:
+        n, _, _ = self.grid_info(what)
+        out = np.zeros(n[0] * n[1] * n[2] * 4)
+        check(lib().mafm_scan_grid_copy(self._h, what, ptr(out)))
+        return out.reshape(n[0], n[1], n[2], 4)
+
+
+def run_batch(scans: list, precision=_abi.FP32C, lanes=0, block=0, tile=0, stream=None):
+    """Relax several scans in one persistent launch; returns (list of points, stats)."""
+    n = len(scans)
+    handles = (C.c_void_p * n)(*[s.handle for s in scans])
+    outs = [np.zeros(s.desc.n_points, dtype=_abi.POINT_DTYPE) for s in scans]
+    optrs = (C.c_void_p * n)(*[o.ctypes.data for o in outs])
+    stats = _abi.RunStats()
+    o = run_opts(precision, lanes, block, tile)
+    check(lib().mafm_run_batch(handles, n, C.byref(o), optrs, C.byref(stats), stream))
+    return outs, stats

@@ -1,0 +1,715 @@
+/*
+ * mafm_oracle.c — ORACLE / TEST INFRASTRUCTURE.  Not part of the product.
+ *
+ * A plain-C, FP64, CPU restatement of the MechAFM scan path, used only as the
+ * checker by tests/, __graft_entry__.smoke() and bench.py's CPU-baseline and
+ * reference legs.  The product (libmafm) never links or calls it.
+ *
+ * It follows the reference's algorithm and floating-point operation order so
+ * that, compiled with -ffp-contract=off, it reproduces the reference's FP64
+ * results.  It is pinned against the reference itself: tests/golden/ holds
+ * outputs of the unmodified reference sources (built by oracle/Makefile `ref`,
+ * driver oracle/ref_dump.cpp) and tests/test_oracle_golden.py checks this file
+ * against them.
+ *
+ * Reference correspondence (SINGROUP/MechAFM, src/):
+ *   pair terms          LJ interactions.cpp:15-27, Morse :29-40, Coulomb :42-51
+ *   tip–dummy coupling  TipHarmonic interactions.cpp:252-266, simulation.cpp:503-515
+ *   force grid lookup   ForceGrid::interpolate force_grid.cpp:88-155, :158-275
+ *   external field      ElectrostaticPotentialInteraction ctor interactions.cpp:53-234,
+ *                       fft.cpp:11-94 (the 3-D DFT here is computed directly from
+ *                       its definition instead of kiss_fft's mixed-radix FFT)
+ *   rigid grid build    Simulation::buildTipGridInteractions simulation.cpp:420-501
+ *   integrators         integrators.cpp:8-111
+ *   minimisers          checkConvergence / SD / FIRE minimiser.cpp:15-129
+ *   scan loop           Simulation::run simulation.cpp:78-122, System::setDummyXY
+ *                       system.cpp:139-162, getOutput system.cpp:28-51
+ */
+#include <math.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <omp.h>
+
+#include "mafm.h"
+
+#define PI 3.14159265358979323846
+#define TOL 1e-10
+
+static char g_err[512];
+const char* oracle_last_error(void) { return g_err; }
+
+typedef struct { double x, y, z; } v3;
+
+typedef struct {
+    double x, y, z, qq, p0, p1, p2;
+    int kind, coul;
+} Term;
+
+typedef struct {
+    int n[3];
+    int periodic, orth;
+    double b[3][3], inv[3][3], origin[3];
+    double* fe; /* 4 per node: Fx Fy Fz E */
+} Grid;
+
+typedef struct {
+    const mafm_scan_desc* d;
+    Term* terms;
+    int nt;
+    int mode; /* 0 pairs, 1 pairs + external field, 2 rigid grid */
+    Grid es, grid;
+    double cell[3][3], cinv[3][3];
+    int err;
+} Ctx;
+
+/* ---- 3x3 helpers, matrices.hpp:89-160 ---------------------------------- */
+static double det3(double (*m)[3]) {
+    double d = 0;
+    d = m[0][0] * (m[1][1] * m[2][2] - m[1][2] * m[2][1]);
+    d += m[0][1] * (m[1][2] * m[2][0] - m[1][0] * m[2][2]);
+    d += m[0][2] * (m[1][0] * m[2][1] - m[1][1] * m[2][0]);
+    return d;
+}
+static void inv3(double (*m)[3], double (*r)[3]) {
+    double inv_det = 1 / det3(m);
+    double a = m[0][0], b = m[0][1], c = m[0][2], d = m[1][0], e = m[1][1], f = m[1][2];
+    double g = m[2][0], h = m[2][1], i = m[2][2];
+    r[0][0] = inv_det * (e * i - f * h);
+    r[0][1] = -inv_det * (b * i - c * h);
+    r[0][2] = inv_det * (b * f - c * e);
+    r[1][0] = -inv_det * (d * i - f * g);
+    r[1][1] = inv_det * (a * i - c * g);
+    r[1][2] = -inv_det * (a * f - c * d);
+    r[2][0] = inv_det * (d * h - e * g);
+    r[2][1] = -inv_det * (a * h - b * g);
+    r[2][2] = inv_det * (a * e - b * d);
+}
+static v3 mulv(double (*m)[3], v3 v) {
+    v3 r;
+    r.x = m[0][0] * v.x + m[0][1] * v.y + m[0][2] * v.z;
+    r.y = m[1][0] * v.x + m[1][1] * v.y + m[1][2] * v.z;
+    r.z = m[2][0] * v.x + m[2][1] * v.y + m[2][2] * v.z;
+    return r;
+}
+static int is_diag(double (*m)[3]) {
+    double ds = 0, nd = 0;
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) {
+            if (i == j) ds += fabs(m[i][i]);
+            else nd += fabs(m[i][j]);
+        }
+    return nd < 1.0e-10 * ds;
+}
+static double len3(v3 v) { return sqrt(v.x * v.x + v.y * v.y + v.z * v.z); }
+
+/* ---- pair terms --------------------------------------------------------- */
+/* r = tip - (atom + shift); the image shift is already in the term position. */
+static void term_vdw(const Term* t, v3 tip, v3* f, double* e) {
+    v3 r = {tip.x - t->x, tip.y - t->y, tip.z - t->z};
+    if (t->kind == MAFM_PAIR_LJ) { /* interactions.cpp:15-27 */
+        double r_sqr = r.x * r.x + r.y * r.y + r.z * r.z;
+        double r6 = r_sqr * r_sqr * r_sqr;
+        double term_a = t->p1 / (r6 * r6);
+        double term_b = t->p0 / r6;
+        *e = term_a - term_b;
+        double s = (12 * term_a - 6 * term_b) / r_sqr;
+        f->x = s * r.x; f->y = s * r.y; f->z = s * r.z;
+    } else { /* Morse, interactions.cpp:29-40 */
+        double rl = len3(r);
+        double d = exp(-t->p1 * (rl - t->p2));
+        *e = t->p0 * (d * d - 2 * d + 1);
+        double f_abs = 2 * t->p0 * t->p1 * (d * d - d);
+        double s = f_abs / rl;
+        f->x = s * r.x; f->y = s * r.y; f->z = s * r.z;
+    }
+}
+static void term_coul(double qq, v3 r, v3* f, double* e) { /* interactions.cpp:42-51 */
+    double rl = len3(r);
+    *e = qq / rl;
+    double s = qq / (rl * rl * rl);
+    f->x = s * r.x; f->y = s * r.y; f->z = s * r.z;
+}
+
+/* ---- trilinear grid lookup, force_grid.cpp:88-275 ----------------------- */
+static int grid_index(Ctx* c, const Grid* g, int x, int y, int z) {
+    if (x < 0 || y < 0 || z < 0 || x >= g->n[0] || y >= g->n[1] || z >= g->n[2]) {
+        if (g->periodic) {
+            int n;
+            if (x < 0 || x >= g->n[0]) { n = (int)floor((double)x / g->n[0]); x -= n * g->n[0]; }
+            if (y < 0 || y >= g->n[1]) { n = (int)floor((double)y / g->n[1]); y -= n * g->n[1]; }
+            if (z < 0 || z >= g->n[2]) { n = (int)floor((double)z / g->n[2]); z -= n * g->n[2]; }
+        } else {
+            c->err |= 2;
+            x = x < 0 ? 0 : (x >= g->n[0] ? g->n[0] - 1 : x);
+            y = y < 0 ? 0 : (y >= g->n[1] ? g->n[1] - 1 : y);
+            z = z < 0 ? 0 : (z >= g->n[2] ? g->n[2] - 1 : z);
+        }
+    }
+    return (x * g->n[1] + y) * g->n[2] + z;
+}
+
+static void grid_interp(Ctx* c, const Grid* g, v3 pos, v3* f, double* e, int* outside) {
+    int gp[3];
+    v3 q = {pos.x - g->origin[0], pos.y - g->origin[1], pos.z - g->origin[2]};
+    v3 pb;
+    if (g->orth) {
+        pb.x = q.x / g->b[0][0]; pb.y = q.y / g->b[1][1]; pb.z = q.z / g->b[2][2];
+    } else {
+        double inv[3][3];
+        memcpy(inv, g->inv, sizeof inv);
+        pb = mulv(inv, q);
+    }
+    gp[0] = (int)floor(pb.x); gp[1] = (int)floor(pb.y); gp[2] = (int)floor(pb.z);
+    if (!g->periodic) {
+        for (int a = 0; a < 3; ++a) {
+            if (gp[a] < 0) { gp[a] = 0; *outside = 1; }
+            else if (gp[a] >= g->n[a]) { gp[a] = g->n[a] - 1; *outside = 1; }
+        }
+    }
+    const double* s[8];
+    for (int i = 0; i < 2; ++i)
+        for (int j = 0; j < 2; ++j)
+            for (int k = 0; k < 2; ++k)
+                s[i * 4 + j * 2 + k] = g->fe + 4 * (size_t)grid_index(c, g, gp[0] + i, gp[1] + j, gp[2] + k);
+    double dx = pb.x - gp[0], dy = pb.y - gp[1], dz = pb.z - gp[2];
+    double out[4];
+    for (int m = 0; m < 4; ++m) {
+        double v00 = s[0][m] * (1 - dx) + s[4][m] * dx;
+        double v01 = s[1][m] * (1 - dx) + s[5][m] * dx;
+        double v10 = s[2][m] * (1 - dx) + s[6][m] * dx;
+        double v11 = s[3][m] * (1 - dx) + s[7][m] * dx;
+        double v0 = v00 * (1 - dy) + v10 * dy;
+        double v1 = v01 * (1 - dy) + v11 * dy;
+        out[m] = v0 * (1 - dz) + v1 * dz;
+    }
+    f->x = out[0]; f->y = out[1]; f->z = out[2]; *e = out[3];
+}
+
+/* ---- force evaluations --------------------------------------------------- */
+/* Tip–surface terms (the interactions with isTipSurface(), system.cpp:41-51). */
+static void eval_ts(Ctx* c, v3 tip, v3* F, double* E, int* outside) {
+    v3 f = {0, 0, 0};
+    double e = 0;
+    F->x = F->y = F->z = 0;
+    *E = 0;
+    if (c->mode == 2) {
+        grid_interp(c, &c->grid, tip, &f, &e, outside);
+        F->x += f.x; F->y += f.y; F->z += f.z; *E += e;
+        return;
+    }
+    for (int i = 0; i < c->nt; ++i) {
+        const Term* t = &c->terms[i];
+        term_vdw(t, tip, &f, &e);
+        F->x += f.x; F->y += f.y; F->z += f.z; *E += e;
+        if (t->coul) {
+            v3 r = {tip.x - t->x, tip.y - t->y, tip.z - t->z};
+            term_coul(t->qq, r, &f, &e);
+            F->x += f.x; F->y += f.y; F->z += f.z; *E += e;
+        }
+    }
+    if (c->mode == 1) {
+        int dummy = 0;
+        grid_interp(c, &c->es, tip, &f, &e, &dummy);
+        F->x += f.x; F->y += f.y; F->z += f.z; *E += e;
+    }
+}
+
+/* All interactions of the relaxation: tip–surface, then the tip–dummy vdW,
+ * optional Coulomb and the XY spring (buildTipDummyInteractions order). */
+static void eval_all(Ctx* c, v3 tip, v3 dum, v3* F, double* E, int* outside) {
+    const mafm_scan_desc* d = c->d;
+    eval_ts(c, tip, F, E, outside);
+    Term td;
+    td.x = tip.x; td.y = tip.y; td.z = tip.z;
+    td.kind = d->dummy_pair.kind;
+    td.p0 = d->dummy_pair.p[0]; td.p1 = d->dummy_pair.p[1]; td.p2 = d->dummy_pair.p[2];
+    v3 f;
+    double e;
+    term_vdw(&td, dum, &f, &e); /* r = dummy - tip; the tip receives -f */
+    F->x -= f.x; F->y -= f.y; F->z -= f.z; *E += e;
+    if (d->tip_dummy_coulomb && d->dummy_charge != 0 && d->tip_charge != 0) {
+        double qq = d->qbase * d->dummy_charge * d->tip_charge;
+        v3 r = {dum.x - tip.x, dum.y - tip.y, dum.z - tip.z};
+        term_coul(qq, r, &f, &e);
+        F->x -= f.x; F->y -= f.y; F->z -= f.z; *E += e;
+    }
+    { /* TipHarmonicInteraction, interactions.cpp:252-266 */
+        double rx = dum.x - tip.x, ry = dum.y - tip.y;
+        double r = sqrt(rx * rx + ry * ry);
+        double dr = r - d->harm_r0;
+        double eh = d->harm_k * dr * dr;
+        double fx = 0, fy = 0;
+        if (r > TOL) {
+            double s = -2 * d->harm_k * dr / r;
+            fx = s * rx; fy = s * ry;
+        }
+        F->x -= fx; F->y -= fy; F->z -= 0.0;
+        *E += eh;
+    }
+}
+
+/* ---- minimisers ---------------------------------------------------------- */
+static int converged(const mafm_scan_desc* d, v3 F, double ediff) {
+    switch (d->minterm) {
+        case MAFM_TERM_E: return fabs(ediff) < d->etol;
+        case MAFM_TERM_F: return len3(F) < d->ftol;
+        default: return fabs(ediff) < d->etol && len3(F) < d->ftol;
+    }
+}
+
+typedef struct {
+    v3 tip, vel, dum;
+    double energy; /* System::energies_[1], carried across z levels */
+    int outside;
+} State;
+
+static int fire(Ctx* c, State* s) {
+    const mafm_scan_desc* d = c->d;
+    const int n_min = 5;
+    const double f_inc = 1.1, f_dec = 0.5, f_a = 0.99, a_start = 0.1;
+    const double dt_max = 10 * d->dt;
+    double alpha = a_start, dt = d->dt;
+    int n_non_neg = 0;
+    int n_tot = 1;
+    for (; n_tot < d->maxsteps; ++n_tot) {
+        double prev = s->energy;
+        v3 F;
+        double E;
+        v3 p = s->tip, v = s->vel;
+        if (d->integrator == MAFM_INT_EULER) {
+            eval_all(c, p, s->dum, &F, &E, &s->outside);
+            s->tip.x = p.x + dt * v.x; s->tip.y = p.y + dt * v.y; s->tip.z = p.z + dt * v.z;
+            s->vel.x = v.x + dt * F.x / 1.0; s->vel.y = v.y + dt * F.y / 1.0; s->vel.z = v.z + dt * F.z / 1.0;
+        } else if (d->integrator == MAFM_INT_MIDPOINT) {
+            v3 f1, f2;
+            double e1, e2;
+            eval_all(c, p, s->dum, &f1, &e1, &s->outside);
+            v3 p2 = {p.x + dt / 2 * v.x, p.y + dt / 2 * v.y, p.z + dt / 2 * v.z};
+            v3 v2 = {v.x + dt / 2 * f1.x / 1.0, v.y + dt / 2 * f1.y / 1.0, v.z + dt / 2 * f1.z / 1.0};
+            eval_all(c, p2, s->dum, &f2, &e2, &s->outside);
+            s->tip.x = p.x + dt * v2.x; s->tip.y = p.y + dt * v2.y; s->tip.z = p.z + dt * v2.z;
+            s->vel.x = v.x + dt * f2.x / 1.0; s->vel.y = v.y + dt * f2.y / 1.0; s->vel.z = v.z + dt * f2.z / 1.0;
+            F = f2;
+            E = e2;
+        } else {
+            v3 f1, f2, f3, f4;
+            double e1, e2, e3, e4;
+            eval_all(c, p, s->dum, &f1, &e1, &s->outside);
+            v3 p2 = {p.x + dt / 2 * v.x, p.y + dt / 2 * v.y, p.z + dt / 2 * v.z};
+            v3 v2 = {v.x + dt / 2 * f1.x / 1.0, v.y + dt / 2 * f1.y / 1.0, v.z + dt / 2 * f1.z / 1.0};
+            eval_all(c, p2, s->dum, &f2, &e2, &s->outside);
+            v3 p3 = {p.x + dt / 2 * v2.x, p.y + dt / 2 * v2.y, p.z + dt / 2 * v2.z};
+            v3 v3_ = {v.x + dt / 2 * f2.x / 1.0, v.y + dt / 2 * f2.y / 1.0, v.z + dt / 2 * f2.z / 1.0};
+            eval_all(c, p3, s->dum, &f3, &e3, &s->outside);
+            v3 p4 = {p.x + dt * v3_.x, p.y + dt * v3_.y, p.z + dt * v3_.z};
+            v3 v4 = {v.x + dt * f3.x / 1.0, v.y + dt * f3.y / 1.0, v.z + dt * f3.z / 1.0};
+            eval_all(c, p4, s->dum, &f4, &e4, &s->outside);
+            s->tip.x = p.x + dt / 6 * (v.x + 2 * v2.x + 2 * v3_.x + v4.x);
+            s->tip.y = p.y + dt / 6 * (v.y + 2 * v2.y + 2 * v3_.y + v4.y);
+            s->tip.z = p.z + dt / 6 * (v.z + 2 * v2.z + 2 * v3_.z + v4.z);
+            s->vel.x = v.x + dt / 6 * (f1.x + 2 * f2.x + 2 * f3.x + f4.x) / 1.0;
+            s->vel.y = v.y + dt / 6 * (f1.y + 2 * f2.y + 2 * f3.y + f4.y) / 1.0;
+            s->vel.z = v.z + dt / 6 * (f1.z + 2 * f2.z + 2 * f3.z + f4.z) / 1.0;
+            F.x = (f1.x + 2 * f2.x + 2 * f3.x + f4.x) / 6;
+            F.y = (f1.y + 2 * f2.y + 2 * f3.y + f4.y) / 6;
+            F.z = (f1.z + 2 * f2.z + 2 * f3.z + f4.z) / 6;
+            E = (e1 + 2 * e2 + 2 * e3 + e4) / 6;
+        }
+        s->energy = E;
+        if (converged(d, F, E - prev)) break;
+        /* Only the tip moves, so P = v_tip . F_tip (minimiser.cpp:107-113). */
+        v3 w = s->vel;
+        double pw = w.x * F.x + w.y * F.y + w.z * F.z;
+        double fl = len3(F);
+        v3 fh = {0, 0, 0};
+        if (fl > 1e-10) { fh.x = F.x / fl; fh.y = F.y / fl; fh.z = F.z / fl; }
+        double vl = len3(w);
+        s->vel.x = (1 - alpha) * w.x + alpha * fh.x * vl;
+        s->vel.y = (1 - alpha) * w.y + alpha * fh.y * vl;
+        s->vel.z = (1 - alpha) * w.z + alpha * fh.z * vl;
+        if (pw < 0) {
+            s->vel.x = s->vel.y = s->vel.z = 0;
+            n_non_neg = 0;
+            dt *= f_dec;
+            alpha = a_start;
+        } else {
+            if (n_non_neg > n_min) {
+                double g = dt * f_inc;
+                dt = g < dt_max ? g : dt_max;
+                alpha *= f_a;
+            }
+            n_non_neg++;
+        }
+    }
+    return n_tot;
+}
+
+static int steepest(Ctx* c, State* s) {
+    const mafm_scan_desc* d = c->d;
+    int n = 1;
+    for (; n < d->maxsteps; ++n) {
+        double prev = s->energy;
+        v3 F;
+        double E;
+        eval_all(c, s->tip, s->dum, &F, &E, &s->outside);
+        s->energy = E;
+        if (converged(d, F, E - prev)) break;
+        s->tip.x += d->dt * F.x; s->tip.y += d->dt * F.y; s->tip.z += d->dt * F.z;
+    }
+    return n;
+}
+
+/* System::setDummyXY (system.cpp:139-162) */
+static void dummy_xy(Ctx* c, int wrap, double x, double y, double* ox, double* oy) {
+    if (wrap) {
+        const mafm_scan_desc* d = c->d;
+        v3 t = {x - d->offset[0], y - d->offset[1], 0 - d->offset[2]};
+        v3 cn = mulv(c->cinv, t);
+        cn.x -= floor(cn.x);
+        cn.y -= floor(cn.y);
+        v3 p = mulv(c->cell, cn);
+        *ox = p.x + d->offset[0];
+        *oy = p.y + d->offset[1];
+    } else {
+        *ox = x;
+        *oy = y;
+    }
+}
+
+/* One pixel column: the loop body of Simulation::run (simulation.cpp:93-122). */
+static void column(Ctx* c, int col, mafm_point* out) {
+    const mafm_scan_desc* d = c->d;
+    const int i = col / d->ny, j = col % d->ny;
+    State s;
+    memset(&s, 0, sizeof s);
+    double x, y;
+    dummy_xy(c, d->tip_pbc && !d->rigidgrid, i * d->dx, j * d->dy, &x, &y);
+    s.dum.x = s.tip.x = x;
+    s.dum.y = s.tip.y = y;
+    s.dum.z = d->zhigh;
+    s.tip.z = d->zhigh - d->tip_dummy_d;
+    for (int k = 0; k < d->nz; ++k) {
+        s.outside = 0;
+        int n = d->minimiser == MAFM_MIN_SD ? steepest(c, &s) : fire(c, &s);
+        mafm_point* p = out + k;
+        v3 F;
+        double E;
+        eval_ts(c, s.tip, &F, &E, &s.outside);
+        p->tip[0] = s.tip.x; p->tip[1] = s.tip.y; p->tip[2] = s.tip.z;
+        p->force[0] = F.x; p->force[1] = F.y; p->force[2] = F.z;
+        p->energy = E;
+        p->steps = n;
+        p->status = (n >= d->maxsteps ? MAFM_PT_MAXSTEPS : 0) | (s.outside ? MAFM_PT_OUTSIDE : 0);
+        if (!isfinite(F.x) || !isfinite(F.y) || !isfinite(F.z) || !isfinite(E))
+            p->status |= MAFM_PT_NONFINITE;
+        s.dum.z -= d->dz;
+        s.tip.z -= d->dz;
+    }
+}
+
+/* ---- 3-D DFT (definition of kiss_fftnd's transform, no normalisation) ---- */
+static void dft_axis(double* re, double* im, const int n[3], int axis, int inverse) {
+    const int L = n[axis];
+    const size_t stride = axis == 0 ? (size_t)n[1] * n[2] : (axis == 1 ? (size_t)n[2] : 1);
+    const size_t total = (size_t)n[0] * n[1] * n[2];
+    double* cs = malloc(sizeof(double) * L);
+    double* sn = malloc(sizeof(double) * L);
+    for (int m = 0; m < L; ++m) {
+        double a = 2 * PI * m / L;
+        cs[m] = cos(a);
+        sn[m] = inverse ? sin(a) : -sin(a);
+    }
+    const size_t nlines = total / L;
+#pragma omp parallel
+    {
+        double* tr = malloc(sizeof(double) * L);
+        double* ti = malloc(sizeof(double) * L);
+#pragma omp for schedule(static)
+        for (long long line = 0; line < (long long)nlines; ++line) {
+            size_t base;
+            if (axis == 0) base = (size_t)line;
+            else if (axis == 1) base = ((size_t)line / n[2]) * (size_t)n[1] * n[2] + (size_t)line % n[2];
+            else base = (size_t)line * n[2];
+            for (int k = 0; k < L; ++k) {
+                double sr = 0, si = 0;
+                for (int m = 0; m < L; ++m) {
+                    int w = (int)(((long long)k * m) % L);
+                    double xr = re[base + m * stride], xi = im[base + m * stride];
+                    sr += xr * cs[w] - xi * sn[w];
+                    si += xr * sn[w] + xi * cs[w];
+                }
+                tr[k] = sr;
+                ti[k] = si;
+            }
+            for (int k = 0; k < L; ++k) {
+                re[base + k * stride] = tr[k];
+                im[base + k * stride] = ti[k];
+            }
+        }
+        free(tr);
+        free(ti);
+    }
+    free(cs);
+    free(sn);
+}
+
+static void dft3(double* re, double* im, const int n[3], int inverse) {
+    for (int a = 0; a < 3; ++a) dft_axis(re, im, n, a, inverse);
+}
+
+/* ElectrostaticPotentialInteraction ctor, interactions.cpp:53-234. */
+static int build_es(Ctx* c) {
+    const mafm_scan_desc* d = c->d;
+    Grid* g = &c->es;
+    for (int a = 0; a < 3; ++a) g->n[a] = d->epot_n[a];
+    for (int r = 0; r < 3; ++r)
+        for (int q = 0; q < 3; ++q) g->b[r][q] = d->epot_basis[3 * r + q];
+    for (int a = 0; a < 3; ++a) g->origin[a] = d->epot_origin[a];
+    g->periodic = 1;
+    g->orth = is_diag(g->b);
+    inv3(g->b, g->inv);
+    const int* n = g->n;
+    const size_t N = (size_t)n[0] * n[1] * n[2];
+    double* rho = calloc(N, sizeof(double));
+    const double w = 0.5; /* g_tip_gaussian_width, globals.hpp:17 */
+    const double w2 = w * w;
+    const double norm = 1.0 / pow(w * sqrt(2.0 * PI), 3);
+    int nmin = n[0] < n[1] ? n[0] : n[1];
+    nmin = nmin < n[2] ? nmin : n[2];
+    int cut[3] = {nmin, nmin, nmin};
+    for (int a = 0; a < 3; ++a) {
+        for (int i = 0; i < nmin - 1; i++) {
+            double vx = i * g->b[0][a], vy = i * g->b[1][a], vz = i * g->b[2][a];
+            double sq = vx * vx + vy * vy + vz * vz;
+            if (exp(-0.5 * sq / w2) < 1.0e-10) { cut[a] = i; break; }
+        }
+    }
+    const double q = d->tip_charge;
+    for (int ix = -cut[0]; ix <= cut[0]; ix++)
+        for (int iy = -cut[1]; iy <= cut[1]; iy++)
+            for (int iz = -cut[2]; iz < cut[2]; iz++) {
+                v3 p;
+                if (g->orth) {
+                    p.x = 0 + ix * g->b[0][0]; p.y = 0 + iy * g->b[1][1]; p.z = 0 + iz * g->b[2][2];
+                } else {
+                    v3 gv = {ix, iy, iz};
+                    v3 m = mulv(g->b, gv);
+                    p.x = 0 + m.x; p.y = 0 + m.y; p.z = 0 + m.z;
+                }
+                double r2 = p.x * p.x + p.y * p.y + p.z * p.z;
+                int x = ix, y = iy, z = iz, k;
+                if (x < 0 || x >= n[0]) { k = (int)floor((double)x / n[0]); x -= k * n[0]; }
+                if (y < 0 || y >= n[1]) { k = (int)floor((double)y / n[1]); y -= k * n[1]; }
+                if (z < 0 || z >= n[2]) { k = (int)floor((double)z / n[2]); z -= k * n[2]; }
+                rho[((size_t)x * n[1] + y) * n[2] + z] += q * norm * exp(-0.5 * r2 / w2);
+            }
+    double* vr = malloc(N * sizeof(double));
+    double* vi = calloc(N, sizeof(double));
+    double* rr = rho;
+    double* ri = calloc(N, sizeof(double));
+    memcpy(vr, d->epot, N * sizeof(double));
+    dft3(vr, vi, n, 0);
+    dft3(rr, ri, n, 0);
+    const double vol = det3(g->b);
+    for (size_t i = 0; i < N; ++i) { /* E(k) = V(k) * vol * rho(k) */
+        double ar = vol * rr[i], ai = vol * ri[i];
+        double er = vr[i] * ar - vi[i] * ai, ei = vr[i] * ai + vi[i] * ar;
+        vr[i] = er;
+        vi[i] = ei;
+    }
+    /* reciprocal basis (B diag(n))^-1^T, fft.cpp:41-47 */
+    double bn[3][3], bi[3][3], kb[3][3];
+    for (int r = 0; r < 3; ++r)
+        for (int q2 = 0; q2 < 3; ++q2) bn[r][q2] = g->b[r][q2] * n[q2];
+    inv3(bn, bi);
+    for (int r = 0; r < 3; ++r)
+        for (int q2 = 0; q2 < 3; ++q2) kb[r][q2] = bi[q2][r];
+    g->fe = malloc(4 * N * sizeof(double));
+    double* tr = malloc(N * sizeof(double));
+    double* ti = malloc(N * sizeof(double));
+    int status = 0;
+    for (int comp = -1; comp < 3 && !status; ++comp) {
+        if (comp < 0) {
+            memcpy(tr, vr, N * sizeof(double));
+            memcpy(ti, vi, N * sizeof(double));
+        } else {
+            for (int ix = 0; ix < n[0]; ix++) {
+                double ka = ix * kb[comp][0];
+                if (ix >= n[0] / 2) ka -= n[0] * kb[comp][0];
+                for (int iy = 0; iy < n[1]; iy++) {
+                    double kbv = iy * kb[comp][1];
+                    if (iy >= n[1] / 2) kbv -= n[1] * kb[comp][1];
+                    for (int iz = 0; iz < n[2]; iz++) {
+                        double kc = iz * kb[comp][2];
+                        if (iz >= n[2] / 2) kc -= n[2] * kb[comp][2];
+                        size_t i = ((size_t)ix * n[1] + iy) * n[2] + iz;
+                        double kk = ka + kbv + kc;
+                        /* -2 pi i k E(k) */
+                        tr[i] = 2 * PI * kk * vi[i];
+                        ti[i] = -2 * PI * kk * vr[i];
+                    }
+                }
+            }
+        }
+        dft3(tr, ti, n, 1);
+        for (size_t i = 0; i < N; ++i) {
+            if (ti[i] / N > 1.0e-8) { /* fft.cpp:79-83 */
+                snprintf(g_err, sizeof g_err,
+                         "Imaginary part of inverse FFT exceeded threshold 1.0e-8! Value: %e", ti[i]);
+                status = MAFM_E_RANGE;
+                break;
+            }
+            g->fe[4 * i + (comp < 0 ? 3 : comp)] = tr[i] / N;
+        }
+    }
+    free(tr); free(ti); free(vr); free(vi); free(rr); free(ri);
+    return status;
+}
+
+/* Simulation::buildTipGridInteractions, simulation.cpp:420-501. */
+static void build_grid(Ctx* c) {
+    const mafm_scan_desc* d = c->d;
+    Grid* g = &c->grid;
+    double sp[3] = {d->dx / 2, d->dy / 2, d->dz / 2};
+    int border[3];
+    for (int a = 0; a < 3; ++a) border[a] = (int)ceil(1.5 / sp[a]);
+    g->n[0] = (int)(floor(d->area[0] / sp[0]) + 2 * border[0] + 1);
+    g->n[1] = (int)(floor(d->area[1] / sp[1]) + 2 * border[1] + 1);
+    g->n[2] = (int)(floor((d->zhigh - d->zlow) / sp[2]) + 2 * border[2] + 1);
+    g->origin[0] = -border[0] * sp[0];
+    g->origin[1] = -border[1] * sp[1];
+    g->origin[2] = d->zlow - d->tip_dummy_d - border[2] * sp[2];
+    memset(g->b, 0, sizeof g->b);
+    for (int a = 0; a < 3; ++a) g->b[a][a] = sp[a];
+    g->orth = 1;
+    g->periodic = 0;
+    const size_t N = (size_t)g->n[0] * g->n[1] * g->n[2];
+    g->fe = malloc(4 * N * sizeof(double));
+    const int saved = c->mode;
+    c->mode = d->use_external_potential ? 1 : 0;
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int i = 0; i < g->n[0]; ++i) {
+        for (int j = 0; j < g->n[1]; ++j) {
+            double x, y;
+            dummy_xy(c, d->tip_pbc, i * sp[0] + g->origin[0], j * sp[1] + g->origin[1], &x, &y);
+            for (int k = 0; k < g->n[2]; ++k) {
+                v3 tip = {x, y, k * sp[2] + g->origin[2]};
+                v3 F;
+                double E;
+                int dummy = 0;
+                eval_ts(c, tip, &F, &E, &dummy);
+                double* o = g->fe + 4 * (((size_t)i * g->n[1] + j) * g->n[2] + k);
+                o[0] = F.x; o[1] = F.y; o[2] = F.z; o[3] = E;
+            }
+        }
+    }
+    c->mode = saved;
+}
+
+static int ctx_init(Ctx* c, const mafm_scan_desc* d) {
+    memset(c, 0, sizeof *c);
+    c->d = d;
+    for (int r = 0; r < 3; ++r)
+        for (int q = 0; q < 3; ++q) c->cell[r][q] = d->cell[3 * r + q];
+    if (d->tip_pbc) inv3(c->cell, c->cinv);
+    const int images = d->vdw_pbc ? 9 : 1;
+    c->nt = d->n_atoms * images;
+    c->terms = malloc(sizeof(Term) * (c->nt > 0 ? c->nt : 1));
+    int t = 0;
+    for (int ia = -1; ia <= 1; ++ia)
+        for (int ib = -1; ib <= 1; ++ib) {
+            if (!d->vdw_pbc && (ia != 0 || ib != 0)) continue;
+            double sx = 0, sy = 0, sz = 0;
+            if (d->vdw_pbc) { /* simulation.cpp:303-306 */
+                sx = ia * c->cell[0][0] + ib * c->cell[0][1];
+                sy = ia * c->cell[1][0] + ib * c->cell[1][1];
+                sz = ia * c->cell[2][0] + ib * c->cell[2][1];
+            }
+            for (int a = 0; a < d->n_atoms; ++a) {
+                Term* tm = &c->terms[t++];
+                const mafm_pair* p = &d->tip_pair[d->type[a]];
+                tm->x = d->pos[3 * a] + sx;
+                tm->y = d->pos[3 * a + 1] + sy;
+                tm->z = d->pos[3 * a + 2] + sz;
+                tm->kind = p->kind;
+                tm->p0 = p->p[0]; tm->p1 = p->p[1]; tm->p2 = p->p[2];
+                tm->coul = d->coulomb && !d->vdw_pbc && d->tip_charge != 0 && d->charge[a] != 0;
+                tm->qq = tm->coul ? d->qbase * d->tip_charge * d->charge[a] : 0.0;
+            }
+        }
+    c->mode = 0;
+    if (d->use_external_potential) {
+        int st = build_es(c);
+        if (st) return st;
+        c->mode = 1;
+    }
+    if (d->rigidgrid) {
+        build_grid(c);
+        c->mode = 2;
+    }
+    return 0;
+}
+
+static void ctx_free(Ctx* c) {
+    free(c->terms);
+    free(c->es.fe);
+    free(c->grid.fe);
+}
+
+/* ---- entry points (ctypes) ----------------------------------------------- */
+
+/* Relax columns [col_begin, col_end); out[(col - col_begin)*nz + k].
+ * nthreads <= 0 keeps the OpenMP default. */
+int oracle_run(const mafm_scan_desc* d, int col_begin, int col_end, mafm_point* out,
+               int nthreads, uint64_t* total_steps) {
+    Ctx c;
+    int st = ctx_init(&c, d);
+    if (st) { ctx_free(&c); return st; }
+    unsigned long long steps = 0;
+#pragma omp parallel for schedule(dynamic, 1) reduction(+ : steps) num_threads(nthreads > 0 ? nthreads : omp_get_max_threads())
+    for (int col = col_begin; col < col_end; ++col) {
+        mafm_point* o = out + (size_t)(col - col_begin) * d->nz;
+        column(&c, col, o);
+        for (int k = 0; k < d->nz; ++k) steps += (unsigned long long)o[k].steps;
+    }
+    if (total_steps) *total_steps = steps;
+    ctx_free(&c);
+    return 0;
+}
+
+/* Tip–surface F,E at tip positions; what 1 = external field only. */
+int oracle_sample(const mafm_scan_desc* d, int what, const double* pts, int64_t n, double* out) {
+    Ctx c;
+    int st = ctx_init(&c, d);
+    if (st) { ctx_free(&c); return st; }
+    for (int64_t i = 0; i < n; ++i) {
+        v3 tip = {pts[3 * i], pts[3 * i + 1], pts[3 * i + 2]};
+        v3 F = {0, 0, 0};
+        double E = 0;
+        int outside = 0;
+        if (what == 1) {
+            if (d->use_external_potential) grid_interp(&c, &c.es, tip, &F, &E, &outside);
+        } else {
+            eval_ts(&c, tip, &F, &E, &outside);
+        }
+        out[4 * i] = F.x; out[4 * i + 1] = F.y; out[4 * i + 2] = F.z; out[4 * i + 3] = E;
+    }
+    ctx_free(&c);
+    return 0;
+}
+
+/* Copy a grid (what 0 = rigid grid, 1 = external field): n, then 4 doubles per node. */
+int oracle_grid(const mafm_scan_desc* d, int what, int32_t n[3], double* out, int64_t cap) {
+    Ctx c;
+    int st = ctx_init(&c, d);
+    if (st) { ctx_free(&c); return st; }
+    const Grid* g = what == 1 ? &c.es : &c.grid;
+    if (!g->fe) { ctx_free(&c); return MAFM_E_INVALID; }
+    for (int a = 0; a < 3; ++a) n[a] = g->n[a];
+    const int64_t N = (int64_t)g->n[0] * g->n[1] * g->n[2] * 4;
+    if (out && cap >= N) memcpy(out, g->fe, (size_t)N * sizeof(double));
+    ctx_free(&c);
+    return 0;
+}
