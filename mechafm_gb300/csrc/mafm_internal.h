@@ -55,7 +55,8 @@ inline void cuda_check(cudaError_t e, const char* what) {
 // Device error bits (mafm_run_stats.error_word, upper half; lower bits are MAFM_PT_*).
 enum : uint32_t {
     ERR_GRID_INDEX = 1u << 16,   // corner outside a non-periodic grid (force_grid.cpp:236-240)
-    ERR_STAGE_TIMEOUT = 1u << 17 // bounded wait on the atom staging barrier expired
+    ERR_STAGE_TIMEOUT = 1u << 17, // bounded wait on the atom staging barrier expired
+    ERR_WATCHDOG = 1u << 18       // a persistent warp ran past its time limit
 };
 
 struct __align__(16) AtomRec64 {
@@ -97,7 +98,7 @@ struct ScanParams {
     const AtomRec32* atoms32;
     // tip–surface source of the relax: 0 pairs, 1 pairs + external field, 2 rigid grid
     int ts_mode;
-    int pad0;
+    int has_coulomb;       // any term carries a Coulomb part
     GridView grid;         // rigid grid (ts_mode 2)
     GridView es;           // external field (ts_mode 1, and grid build)
     // tip–dummy coupling (buildTipDummyInteractions, simulation.cpp:503-515)
@@ -127,29 +128,40 @@ struct RunCounters {
     unsigned int pad;
 };
 
-// Launchers implemented in relax64.cu / relax32.cu.
+// Launchers implemented in relax64.cu / relax32.cu.  ctr points to zeroed
+// device counters owned by the caller.
 cudaError_t launch_relax64(const ScanParams& p, mafm_point* out, RunCounters* ctr,
-                           int col_begin, int col_end, int block, cudaStream_t s);
+                           int col_begin, int col_end, cudaStream_t s);
 cudaError_t launch_sample64(const ScanParams& p, int what, const double* pts, int64_t n,
-                            double* out, cudaStream_t s);
+                            double* out, RunCounters* ctr, cudaStream_t s);
 cudaError_t launch_grid_build64(const ScanParams& p, const GridView& g, Node64* out,
-                                cudaStream_t s);
+                                RunCounters* ctr, cudaStream_t s);
 
 // One entry of a multi-scan work list for the FP32 persistent kernel.
 struct BatchScan {
     ScanParams p;
-    mafm_point* out;
+    mafm_point* out;          // points of columns [col_begin, col_end), (col-col_begin)*nz+k
     long long tile_begin;     // first global tile index of this scan
     int col_begin, col_end;
+    int n_pairs_per_eval;     // vdW + Coulomb terms per force evaluation
+    int has_coulomb;
+};
+
+struct Relax32Config {
+    int lanes;                // lanes per column (1,2,4,8,16,32)
+    int block;                // threads per block
+    int cols_per_tile;        // columns per warp work tile
+    int smem_terms;           // terms staged per warp (larger scans read global memory)
+    int blocks;               // 0 = fill the GPU
+    double watchdog_s;        // persistent-kernel time limit (0 = 600 s)
 };
 
 cudaError_t launch_relax32(const BatchScan* scans_dev, int n_scans, long long n_tiles,
-                           int cols_per_tile, int lanes, int block, int max_terms,
-                           RunCounters* ctr, cudaStream_t s);
+                           const Relax32Config& cfg, RunCounters* ctr, cudaStream_t s);
 cudaError_t launch_sample32(const ScanParams& p, int what, const double* pts, int64_t n,
-                            double* out, cudaStream_t s);
+                            double* out, RunCounters* ctr, cudaStream_t s);
 cudaError_t launch_grid_build32(const ScanParams& p, const GridView& g, float4* out,
-                                cudaStream_t s);
-int relax32_smem_terms_limit(int block);
+                                RunCounters* ctr, cudaStream_t s);
+int sm_count();
 
 }  // namespace mafm

@@ -1,0 +1,970 @@
+// relax32.cu — the FP32-compensated GPU path (precision MAFM_FP32C).
+//
+// Persistent, multi-scan relaxation kernel.  Work is a list of tiles of pixel
+// columns, possibly from many scans (a batch); each warp takes one tile at a
+// time with an atomic counter, and G lanes share one column (G = 1..32, a
+// launch parameter picked by the autotuner).  The warp's current scan's
+// tip–atom terms are staged into the warp's slice of shared memory with a
+// bulk copy (cp.async.bulk + mbarrier); every lane of a group sums its share
+// of the terms, then the group combines its sums with xor shuffles.
+//
+// The main loop runs in "slots": one force evaluation per group per slot,
+// then a per-group state machine advances FIRE/SD and the integrator
+// (euler 1, midpoint 2, rk4 4 evaluations per step).  The evaluation that
+// produces a point's output (System::getOutput, system.cpp:28-51) is one more
+// slot, so lanes never wait on a divergent extra pair loop.
+//
+// Precision: pair terms in FP32 (fast reciprocal refined by one Newton step,
+// fast rsqrt/exp); tip positions in double-float (hi + lo FP32) so that
+// tip–atom separations keep ~1e-7 relative accuracy; per-lane sums compensated
+// (two-sum over chunks of terms); the energy behind the e/ef convergence test
+// and the tip–dummy XY spring are FP64.
+//
+// Reference correspondence (src/): as relax64.cu — interactions.cpp:15-51,
+// 244-266; force_grid.cpp:88-275; integrators.cpp:8-111; minimiser.cpp:15-129;
+// simulation.cpp:93-122, 420-501; system.cpp:28-51, 139-162.
+#include <cstdint>
+
+#include "mafm_internal.h"
+
+namespace mafm {
+namespace {
+
+constexpr unsigned kFull = 0xffffffffu;
+constexpr int kChunk = 4;                 // terms summed plainly before a compensated add
+constexpr long long kWaitLimit = 1ll << 24;  // bounded mbarrier wait (iterations)
+
+enum : int { PH_EVAL0 = 0, PH_EVAL1 = 1, PH_EVAL2 = 2, PH_EVAL3 = 3, PH_OUT = 4 };
+
+// ---------------------------------------------------------------- helpers ----
+
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+    s = a + b;
+    const float bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
+}
+
+struct DF {   // double-float value hi + lo
+    float hi, lo;
+};
+
+__device__ __forceinline__ DF df_split(double x) {
+    const float h = (float)x;
+    return DF{h, (float)(x - (double)h)};
+}
+
+__device__ __forceinline__ double df_val(DF a) { return (double)a.hi + (double)a.lo; }
+
+// a + b for a small float b
+__device__ __forceinline__ DF df_add(DF a, float b) {
+    float s, e;
+    two_sum(a.hi, b, s, e);
+    e += a.lo;
+    const float h = s + e;
+    return DF{h, e - (h - s)};
+}
+
+__device__ __forceinline__ float rcp_nr(float x) {
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    const float e = fmaf(-x, r, 1.0f);
+    return fmaf(r, e, r);
+}
+
+__device__ __forceinline__ float rsqrt_fast(float x) {
+    float r;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
+// Compensated accumulator of {Fx, Fy, Fz, E}.
+struct Acc {
+    float s[4], c[4];
+    __device__ __forceinline__ void zero() {
+#pragma unroll
+        for (int m = 0; m < 4; ++m) s[m] = c[m] = 0.f;
+    }
+    __device__ __forceinline__ void add(const float v[4]) {
+#pragma unroll
+        for (int m = 0; m < 4; ++m) {
+            float t, e;
+            two_sum(s[m], v[m], t, e);
+            s[m] = t;
+            c[m] += e;
+        }
+    }
+    // Combine across the G lanes of a group; every lane ends with the same sums
+    // (two-sum and + are commutative, so partners compute identical values).
+    template <int G>
+    __device__ __forceinline__ void group_reduce() {
+#pragma unroll
+        for (int off = G / 2; off > 0; off >>= 1) {
+#pragma unroll
+            for (int m = 0; m < 4; ++m) {
+                const float so = __shfl_xor_sync(kFull, s[m], off);
+                const float co = __shfl_xor_sync(kFull, c[m], off);
+                float t, e;
+                two_sum(s[m], so, t, e);
+                s[m] = t;
+                c[m] = (c[m] + co) + e;
+            }
+        }
+    }
+};
+
+// One tip–atom term: LJ or Morse (interactions.cpp:15-40) plus Coulomb
+// (:42-51, qq = 0 when absent).  d = tip - atom.
+__device__ __forceinline__ void pair32(const AtomRec32& t, float dx, float dy, float dz,
+                                       bool coul, float v[4]) {
+    const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+    float fs, e;
+    if (__float_as_int(t.b.w) == MAFM_PAIR_LJ) {
+        const float ir2 = rcp_nr(r2);
+        const float ir6 = ir2 * ir2 * ir2;
+        const float t6 = t.b.x * ir6;
+        const float t12 = t.b.y * ir6 * ir6;
+        e = t12 - t6;
+        fs = fmaf(12.f, t12, -6.f * t6) * ir2;
+    } else {
+        const float ir = rsqrt_fast(r2);
+        const float r = r2 * ir;
+        const float d = __expf(-t.b.y * (r - t.b.z));
+        const float dm1 = d - 1.f;
+        e = t.b.x * dm1 * dm1;
+        fs = 2.f * t.b.x * t.b.y * d * dm1 * ir;
+    }
+    if (coul) {
+        const float ir = rsqrt_fast(r2);
+        const float ec = t.a.w * ir;
+        fs = fmaf(ec * ir, ir, fs);
+        e += ec;
+    }
+    v[0] = fmaf(fs, dx, v[0]);
+    v[1] = fmaf(fs, dy, v[1]);
+    v[2] = fmaf(fs, dz, v[2]);
+    v[3] += e;
+}
+
+// Trilinear lookup on an FP32 grid (ForceGrid::interpolate).  q = position -
+// grid origin.  Sets *outside when clamped, ERR_GRID_INDEX when a corner of a
+// non-periodic grid falls outside (then clamped, never read out of bounds).
+__device__ void interp32(const GridView& g, float qx, float qy, float qz, float v[4],
+                         int& outside, unsigned& err) {
+    float pb[3];
+    if (g.orthogonal) {
+        pb[0] = qx / (float)g.basis[0];
+        pb[1] = qy / (float)g.basis[4];
+        pb[2] = qz / (float)g.basis[8];
+    } else {
+        pb[0] = (float)g.inv[0] * qx + (float)g.inv[1] * qy + (float)g.inv[2] * qz;
+        pb[1] = (float)g.inv[3] * qx + (float)g.inv[4] * qy + (float)g.inv[5] * qz;
+        pb[2] = (float)g.inv[6] * qx + (float)g.inv[7] * qy + (float)g.inv[8] * qz;
+    }
+    int gp[3];
+    float d[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        gp[a] = (int)floorf(pb[a]);
+        if (!g.periodic) {
+            if (gp[a] < 0) { gp[a] = 0; outside = 1; }
+            else if (gp[a] >= g.n[a]) { gp[a] = g.n[a] - 1; outside = 1; }
+        }
+        d[a] = pb[a] - (float)gp[a];
+    }
+    int lo[3], hi[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        int x0 = gp[a], x1 = gp[a] + 1;
+        if (g.periodic) {
+            x0 %= g.n[a]; if (x0 < 0) x0 += g.n[a];
+            x1 %= g.n[a]; if (x1 < 0) x1 += g.n[a];
+        } else if (x1 >= g.n[a]) {
+            err |= ERR_GRID_INDEX;
+            x1 = g.n[a] - 1;
+        }
+        lo[a] = x0;
+        hi[a] = x1;
+    }
+    const long long n12 = (long long)g.n[1] * g.n[2];
+    const float4* G4 = g.g32;
+    float4 s[8];
+#pragma unroll
+    for (int c = 0; c < 8; ++c) {
+        const int x = (c >> 2) ? hi[0] : lo[0];
+        const int y = ((c >> 1) & 1) ? hi[1] : lo[1];
+        const int z = (c & 1) ? hi[2] : lo[2];
+        s[c] = __ldg(G4 + (long long)x * n12 + (long long)y * g.n[2] + z);
+    }
+    const float dx = d[0], dy = d[1], dz = d[2];
+    auto lerp3 = [&](float a0, float a1, float a2, float a3, float a4, float a5, float a6, float a7) {
+        const float v00 = a0 * (1 - dx) + a4 * dx, v01 = a1 * (1 - dx) + a5 * dx;
+        const float v10 = a2 * (1 - dx) + a6 * dx, v11 = a3 * (1 - dx) + a7 * dx;
+        const float v0 = v00 * (1 - dy) + v10 * dy, v1 = v01 * (1 - dy) + v11 * dy;
+        return v0 * (1 - dz) + v1 * dz;
+    };
+    v[0] += lerp3(s[0].x, s[1].x, s[2].x, s[3].x, s[4].x, s[5].x, s[6].x, s[7].x);
+    v[1] += lerp3(s[0].y, s[1].y, s[2].y, s[3].y, s[4].y, s[5].y, s[6].y, s[7].y);
+    v[2] += lerp3(s[0].z, s[1].z, s[2].z, s[3].z, s[4].z, s[5].z, s[6].z, s[7].z);
+    v[3] += lerp3(s[0].w, s[1].w, s[2].w, s[3].w, s[4].w, s[5].w, s[6].w, s[7].w);
+}
+
+// Position minus a grid origin, from a double-float position.
+__device__ __forceinline__ void rel_origin(const GridView& g, DF px, DF py, DF pz, float& qx,
+                                           float& qy, float& qz) {
+    const DF ox = df_split(g.origin[0]), oy = df_split(g.origin[1]), oz = df_split(g.origin[2]);
+    qx = (px.hi - ox.hi) + (px.lo - ox.lo);
+    qy = (py.hi - oy.hi) + (py.lo - oy.lo);
+    qz = (pz.hi - oz.hi) + (pz.lo - oz.lo);
+}
+
+// System::setDummyXY (system.cpp:139-162) in FP64.
+__device__ __forceinline__ void dummy_xy(const ScanParams& p, bool wrap, double x, double y,
+                                         double& ox, double& oy) {
+    if (wrap) {
+        const double* ci = p.cell_inv;
+        const double* c = p.cell;
+        const double tx = x - p.offset[0], ty = y - p.offset[1], tz = 0 - p.offset[2];
+        double cx = ci[0] * tx + ci[1] * ty + ci[2] * tz;
+        double cy = ci[3] * tx + ci[4] * ty + ci[5] * tz;
+        const double cz = ci[6] * tx + ci[7] * ty + ci[8] * tz;
+        cx -= floor(cx);
+        cy -= floor(cy);
+        ox = (c[0] * cx + c[1] * cy + c[2] * cz) + p.offset[0];
+        oy = (c[3] * cx + c[4] * cy + c[5] * cz) + p.offset[1];
+    } else {
+        ox = x;
+        oy = y;
+    }
+}
+
+// vdW term of the dummy–tip pair in FP32; r = dummy - tip.
+__device__ __forceinline__ void td_vdw32(const ScanParams& p, float rx, float ry, float rz,
+                                         float f[3], float& e) {
+    const float r2 = rx * rx + ry * ry + rz * rz;
+    float fs;
+    if (p.td_kind == MAFM_PAIR_LJ) {
+        const float ir2 = rcp_nr(r2);
+        const float ir6 = ir2 * ir2 * ir2;
+        const float t6 = (float)p.td_p[0] * ir6;
+        const float t12 = (float)p.td_p[1] * ir6 * ir6;
+        e = t12 - t6;
+        fs = fmaf(12.f, t12, -6.f * t6) * ir2;
+    } else {
+        const float ir = rsqrt_fast(r2);
+        const float r = r2 * ir;
+        const float d = __expf(-(float)p.td_p[1] * (r - (float)p.td_p[2]));
+        const float dm1 = d - 1.f;
+        e = (float)p.td_p[0] * dm1 * dm1;
+        fs = 2.f * (float)p.td_p[0] * (float)p.td_p[1] * d * dm1 * ir;
+    }
+    if (p.td_coul) {
+        const float ir = rsqrt_fast(r2);
+        const float ec = (float)p.td_qq * ir;
+        fs = fmaf(ec * ir, ir, fs);
+        e += ec;
+    }
+    f[0] = fs * rx;
+    f[1] = fs * ry;
+    f[2] = fs * rz;
+}
+
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// ---------------------------------------------------------------- staging ----
+
+struct WarpHdr {
+    unsigned long long mbar;
+    int assign[32];
+    int pad[2];
+};
+static_assert(sizeof(WarpHdr) % 16 == 0, "warp header keeps the atom slice 16-byte aligned");
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint32_t mbar, uint32_t phase) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(mbar), "r"(phase)
+        : "memory");
+    return ok != 0;
+}
+
+// Bulk-copy `bytes` (multiple of 16) of terms into the warp's slice; all lanes
+// wait on the warp's mbarrier with a bounded spin.  Returns false on timeout.
+__device__ bool stage_terms(WarpHdr* hdr, AtomRec32* dst, const AtomRec32* src, int n,
+                            uint32_t& phase, int lane) {
+    const uint32_t bytes = (uint32_t)n * (uint32_t)sizeof(AtomRec32);
+    const uint32_t mbar = smem_addr(&hdr->mbar);
+    __syncwarp();
+    if (lane == 0) {
+        // Order this warp's earlier generic reads of the slice before the async writes.
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mbar),
+                     "r"(bytes)
+                     : "memory");
+        uint64_t gsrc;
+        asm("cvta.to.global.u64 %0, %1;" : "=l"(gsrc) : "l"(src));
+        const uint32_t d0 = smem_addr(dst);
+        constexpr uint32_t kPiece = 32768;
+        for (uint32_t off = 0; off < bytes; off += kPiece) {
+            const uint32_t len = bytes - off < kPiece ? bytes - off : kPiece;
+            asm volatile(
+                "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                    d0 + off),
+                "l"(gsrc + off), "r"(len), "r"(mbar)
+                : "memory");
+        }
+    }
+    long long it = 0;
+    bool ok = true;
+    while (!mbar_try_wait(mbar, phase)) {
+        if (++it > kWaitLimit) {
+            ok = false;
+            break;
+        }
+    }
+    if (!ok) {
+        // Give the copy a second bounded chance to land before the warp leaves.
+        for (long long k = 0; k < kWaitLimit && !mbar_try_wait(mbar, phase); ++k) {
+        }
+    }
+    phase ^= 1u;
+    __syncwarp();
+    return ok;
+}
+
+// ------------------------------------------------------------ the kernel ----
+
+struct GroupState {
+    int col;          // column (scan-relative), -1 idle, -2 no more work
+    int k;            // z level
+    int phase;
+    int n_tot;        // FIRE / SD step counter
+    int nnn;          // FIRE steps since the last P<0
+    float fdt, alpha;
+    DF px, py, pz;    // tip
+    DF ex, ey, ez;    // evaluation position of this slot
+    float vx, vy, vz;
+    float ux, uy, uz; // midpoint v2 / rk4 v_k
+    float sx, sy, sz; // rk4 sum of velocities
+    float gx, gy, gz; // rk4 sum of forces / midpoint f1 unused
+    double esum;      // rk4 sum of energies
+    double e_last;    // System::energies_[1] of the last step
+    DF dx_, dy_;      // dummy xy
+    double dz64;      // dummy z
+    int outside;
+};
+
+template <int G>
+__global__ void __launch_bounds__(256) relax32_kernel(const BatchScan* __restrict__ scans,
+                                                      int n_scans, long long n_tiles,
+                                                      int cols_per_tile, int smem_terms,
+                                                      unsigned long long watchdog_ns,
+                                                      RunCounters* ctr) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int grp = lane / G, lg = lane % G;
+    constexpr int kGroups = 32 / G;
+    const size_t slice = sizeof(WarpHdr) + (size_t)smem_terms * sizeof(AtomRec32);
+    WarpHdr* hdr = reinterpret_cast<WarpHdr*>(smem_raw + (size_t)warp * slice);
+    AtomRec32* sm_terms = reinterpret_cast<AtomRec32*>(hdr + 1);
+
+    if (lane == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&hdr->mbar)) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncwarp();
+    uint32_t phase = 0;
+
+    // warp-uniform state
+    int cur = -1;                 // current scan
+    int t_next = 0, t_end = 0;    // column cursor of the current tile
+    long long pending = -1;       // next tile, of another scan
+    bool exhausted = false;
+    const BatchScan* S = nullptr;
+    const AtomRec32* terms = nullptr;
+    int n_terms = 0;
+    bool coul = false;
+
+    unsigned err = 0;
+    unsigned long long my_steps = 0, my_evals = 0, my_pairs = 0;
+    unsigned status_or = 0;
+
+    GroupState g;
+    g.col = -1;
+    g.ex = g.ey = g.ez = DF{0.f, 0.f};
+
+    auto scan_of_tile = [&](long long t) {
+        int lo = 0, hi = n_scans - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (scans[mid].tile_begin <= t) lo = mid;
+            else hi = mid - 1;
+        }
+        return lo;
+    };
+
+    auto start_level = [&](const ScanParams& P) {
+        g.fdt = (float)P.dt;
+        g.alpha = 0.1f;
+        g.nnn = 0;
+        g.n_tot = 1;
+        g.outside = 0;
+        g.phase = P.maxsteps <= 1 ? PH_OUT : PH_EVAL0;
+        g.ex = g.px; g.ey = g.py; g.ez = g.pz;
+    };
+
+    auto start_column = [&](const ScanParams& P, int c) {
+        g.col = c;
+        g.k = 0;
+        const int i = c / P.ny, j = c % P.ny;
+        double x, y;
+        dummy_xy(P, P.tip_pbc && P.ts_mode != 2, i * P.dx, j * P.dy, x, y);
+        g.dx_ = df_split(x);
+        g.dy_ = df_split(y);
+        g.dz64 = P.zhigh;
+        g.px = g.dx_;
+        g.py = g.dy_;
+        g.pz = df_split(P.zhigh - P.tip_dummy_d);
+        g.vx = g.vy = g.vz = 0.f;
+        g.e_last = 0.0;
+        g.k = 0;
+        start_level(P);
+    };
+
+    // Watchdog: a warp that runs longer than watchdog_ns stops with ERR_WATCHDOG
+    // instead of holding the GPU (checked every 256 slots and scheduling rounds).
+    const unsigned long long t_start = global_ns();
+    unsigned ticks = 0;
+    auto expired = [&]() -> bool {
+        if ((++ticks & 255u) != 0) return false;
+        const bool late = global_ns() - t_start > watchdog_ns;
+        return __any_sync(kFull, late) != 0;
+    };
+
+    bool alive = true;
+    while (alive) {
+        // ---------------- scheduling (warp-collective) ----------------
+        for (;;) {
+            if (expired()) {
+                err |= ERR_WATCHDOG;
+                alive = false;
+                break;
+            }
+            const unsigned need = __ballot_sync(kFull, lg == 0 && g.col == -1);
+            if (need) {
+                if (lane == 0) {
+                    for (int gi = 0; gi < kGroups; ++gi) {
+                        if (!(need & (1u << (gi * G)))) continue;
+                        int a = -1;
+                        for (;;) {
+                            if (t_next < t_end) { a = t_next++; break; }
+                            if (pending >= 0) { a = -1; break; }
+                            if (exhausted) { a = -2; break; }
+                            const long long t = (long long)atomicAdd(&ctr->next_work, 1ull);
+                            if (t >= n_tiles) { exhausted = true; continue; }
+                            const int s = scan_of_tile(t);
+                            if (s == cur) {
+                                const BatchScan& B = scans[s];
+                                t_next = B.col_begin + (int)(t - B.tile_begin) * cols_per_tile;
+                                t_end = min(B.col_end, t_next + cols_per_tile);
+                                continue;
+                            }
+                            pending = t;
+                        }
+                        hdr->assign[gi] = a;
+                    }
+                }
+                __syncwarp();
+                t_next = __shfl_sync(kFull, t_next, 0);
+                t_end = __shfl_sync(kFull, t_end, 0);
+                pending = __shfl_sync(kFull, pending, 0);
+                exhausted = __shfl_sync(kFull, (int)exhausted, 0) != 0;
+                if (g.col == -1) {
+                    const int a = hdr->assign[grp];
+                    if (a >= 0) start_column(S->p, a);
+                    else if (a == -2) g.col = -2;
+                }
+                __syncwarp();
+            }
+            if (__any_sync(kFull, g.col >= 0)) break;
+            if (pending >= 0) {
+                // Every group is idle: switch the warp to the pending tile's scan.
+                const int s = scan_of_tile(pending);
+                cur = s;
+                S = scans + s;
+                const BatchScan& B = *S;
+                t_next = B.col_begin + (int)(pending - B.tile_begin) * cols_per_tile;
+                t_end = min(B.col_end, t_next + cols_per_tile);
+                pending = -1;
+                n_terms = B.p.n_terms_direct;
+                coul = B.has_coulomb != 0;
+                if (n_terms > 0 && n_terms <= smem_terms) {
+                    if (!stage_terms(hdr, sm_terms, B.p.atoms32, n_terms, phase, lane)) {
+                        err |= ERR_STAGE_TIMEOUT;
+                        alive = false;
+                        break;
+                    }
+                    terms = sm_terms;
+                } else {
+                    terms = B.p.atoms32;
+                }
+                if (g.col == -2) g.col = -1;   // groups that found nothing may retry
+                continue;
+            }
+            if (exhausted) {
+                alive = false;
+                break;
+            }
+        }
+        if (!alive) break;
+
+        const ScanParams& P = S->p;
+        const bool working = g.col >= 0;
+
+        // ---------------- one force evaluation per group ----------------
+        Acc acc;
+        acc.zero();
+        {
+            const DF ex = g.ex, ey = g.ey, ez = g.ez;
+            for (int j0 = lg; j0 < n_terms; j0 += G * kChunk) {
+                float v[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+                for (int u = 0; u < kChunk; ++u) {
+                    const int j = j0 + u * G;
+                    if (j < n_terms) {
+                        const AtomRec32 t = terms[j];
+                        const float dx = (ex.hi - t.a.x) + ex.lo;
+                        const float dy = (ey.hi - t.a.y) + ey.lo;
+                        const float dz = (ez.hi - t.a.z) + ez.lo;
+                        pair32(t, dx, dy, dz, coul, v);
+                    }
+                }
+                acc.add(v);
+            }
+        }
+        if (G > 1) acc.template group_reduce<G>();
+
+        if (working) {
+            float v[4] = {0.f, 0.f, 0.f, 0.f};
+            if (P.ts_mode == 1) {
+                float qx, qy, qz;
+                rel_origin(P.es, g.ex, g.ey, g.ez, qx, qy, qz);
+                int unused = 0;
+                interp32(P.es, qx, qy, qz, v, unused, err);
+            } else if (P.ts_mode == 2) {
+                float qx, qy, qz;
+                rel_origin(P.grid, g.ex, g.ey, g.ez, qx, qy, qz);
+                interp32(P.grid, qx, qy, qz, v, g.outside, err);
+            }
+            if (P.ts_mode != 0) acc.add(v);
+            my_evals += (lg == 0);
+            my_pairs += (lg == 0) ? (unsigned long long)S->n_pairs_per_eval : 0ull;
+
+            const float Fsx = acc.s[0] + acc.c[0], Fsy = acc.s[1] + acc.c[1], Fsz = acc.s[2] + acc.c[2];
+            const double Es = (double)acc.s[3] + (double)acc.c[3];
+
+            if (g.phase == PH_OUT) {
+                // Output record of this level (System::getOutput).
+                const int n = g.n_tot;
+                int st = (n >= P.maxsteps ? MAFM_PT_MAXSTEPS : 0) | (g.outside ? MAFM_PT_OUTSIDE : 0);
+                const double Fx = (double)acc.s[0] + (double)acc.c[0];
+                const double Fy = (double)acc.s[1] + (double)acc.c[1];
+                const double Fz = (double)acc.s[2] + (double)acc.c[2];
+                if (!isfinite(Fx) || !isfinite(Fy) || !isfinite(Fz) || !isfinite(Es)) st |= MAFM_PT_NONFINITE;
+                if (lg == 0) {
+                    mafm_point r;
+                    r.tip[0] = df_val(g.px);
+                    r.tip[1] = df_val(g.py);
+                    r.tip[2] = df_val(g.pz);
+                    r.force[0] = Fx;
+                    r.force[1] = Fy;
+                    r.force[2] = Fz;
+                    r.energy = Es;
+                    r.steps = n;
+                    r.status = st;
+                    S->out[(size_t)(g.col - S->col_begin) * P.nz + g.k] = r;
+                    my_steps += (unsigned long long)n;
+                    status_or |= (unsigned)st;
+                }
+                // System::lowerTip (system.hpp:51-54)
+                g.dz64 -= P.dz;
+                {
+                    const DF dzs = df_split(-P.dz);
+                    DF z = df_add(g.pz, dzs.hi);
+                    g.pz = df_add(z, dzs.lo);
+                }
+                g.k++;
+                if (g.k >= P.nz) g.col = -1;
+                else start_level(P);
+            } else {
+                // Full evaluation: add the tip–dummy coupling (simulation.cpp:503-515).
+                const DF dzf = df_split(g.dz64);
+                const float rx = (g.dx_.hi - g.ex.hi) + (g.dx_.lo - g.ex.lo);
+                const float ry = (g.dy_.hi - g.ey.hi) + (g.dy_.lo - g.ey.lo);
+                const float rz = (dzf.hi - g.ez.hi) + (dzf.lo - g.ez.lo);
+                float ftd[3], etd;
+                td_vdw32(P, rx, ry, rz, ftd, etd);
+                // XY spring in FP64 (interactions.cpp:252-266)
+                const double drx = rx, dry = ry;
+                const double rr2 = drx * drx + dry * dry;
+                double eh, hx = 0.0, hy = 0.0;
+                if (P.harm_r0 == 0.0) {
+                    eh = P.harm_k * rr2;
+                    if (rr2 > 1e-20) { hx = -2 * P.harm_k * drx; hy = -2 * P.harm_k * dry; }
+                } else {
+                    const double rr = sqrt(rr2);
+                    const double dr = rr - P.harm_r0;
+                    eh = P.harm_k * dr * dr;
+                    if (rr > 1e-10) {
+                        const double s = -2 * P.harm_k * dr / rr;
+                        hx = s * drx;
+                        hy = s * dry;
+                    }
+                }
+                float Fx, Fy, Fz;
+                {
+                    float t, e;
+                    two_sum(acc.s[0], -ftd[0], t, e);
+                    Fx = t + (acc.c[0] + e) - (float)hx;
+                    two_sum(acc.s[1], -ftd[1], t, e);
+                    Fy = t + (acc.c[1] + e) - (float)hy;
+                    two_sum(acc.s[2], -ftd[2], t, e);
+                    Fz = t + (acc.c[2] + e);
+                }
+                const double E = Es + (double)etd + eh;
+                (void)Fsx; (void)Fsy; (void)Fsz;
+
+                bool step_done = false;
+                float SFx = Fx, SFy = Fy, SFz = Fz;
+                double SE = E;
+                const float dt = g.fdt;
+                if (P.minimiser == MAFM_MIN_SD) {
+                    step_done = true;
+                } else if (P.integrator == MAFM_INT_EULER) {
+                    g.px = df_add(g.px, dt * g.vx);
+                    g.py = df_add(g.py, dt * g.vy);
+                    g.pz = df_add(g.pz, dt * g.vz);
+                    g.vx = fmaf(dt, Fx, g.vx); g.vy = fmaf(dt, Fy, g.vy); g.vz = fmaf(dt, Fz, g.vz);
+                    step_done = true;
+                } else if (P.integrator == MAFM_INT_MIDPOINT) {
+                    if (g.phase == PH_EVAL0) {
+                        const float h = 0.5f * dt;
+                        g.ux = fmaf(h, Fx, g.vx); g.uy = fmaf(h, Fy, g.vy); g.uz = fmaf(h, Fz, g.vz);
+                        g.ex = df_add(g.px, h * g.vx);
+                        g.ey = df_add(g.py, h * g.vy);
+                        g.ez = df_add(g.pz, h * g.vz);
+                        g.phase = PH_EVAL1;
+                    } else {
+                        g.px = df_add(g.px, dt * g.ux);
+                        g.py = df_add(g.py, dt * g.uy);
+                        g.pz = df_add(g.pz, dt * g.uz);
+                        g.vx = fmaf(dt, Fx, g.vx); g.vy = fmaf(dt, Fy, g.vy); g.vz = fmaf(dt, Fz, g.vz);
+                        step_done = true;
+                    }
+                } else {   // RK4
+                    const float h = 0.5f * dt;
+                    if (g.phase == PH_EVAL0) {
+                        g.gx = Fx; g.gy = Fy; g.gz = Fz; g.esum = E;
+                        g.sx = g.vx; g.sy = g.vy; g.sz = g.vz;
+                        g.ex = df_add(g.px, h * g.vx); g.ey = df_add(g.py, h * g.vy); g.ez = df_add(g.pz, h * g.vz);
+                        g.ux = fmaf(h, Fx, g.vx); g.uy = fmaf(h, Fy, g.vy); g.uz = fmaf(h, Fz, g.vz);
+                        g.phase = PH_EVAL1;
+                    } else if (g.phase == PH_EVAL1) {
+                        g.gx = fmaf(2.f, Fx, g.gx); g.gy = fmaf(2.f, Fy, g.gy); g.gz = fmaf(2.f, Fz, g.gz);
+                        g.esum += 2.0 * E;
+                        g.sx = fmaf(2.f, g.ux, g.sx); g.sy = fmaf(2.f, g.uy, g.sy); g.sz = fmaf(2.f, g.uz, g.sz);
+                        g.ex = df_add(g.px, h * g.ux); g.ey = df_add(g.py, h * g.uy); g.ez = df_add(g.pz, h * g.uz);
+                        g.ux = fmaf(h, Fx, g.vx); g.uy = fmaf(h, Fy, g.vy); g.uz = fmaf(h, Fz, g.vz);
+                        g.phase = PH_EVAL2;
+                    } else if (g.phase == PH_EVAL2) {
+                        g.gx = fmaf(2.f, Fx, g.gx); g.gy = fmaf(2.f, Fy, g.gy); g.gz = fmaf(2.f, Fz, g.gz);
+                        g.esum += 2.0 * E;
+                        g.sx = fmaf(2.f, g.ux, g.sx); g.sy = fmaf(2.f, g.uy, g.sy); g.sz = fmaf(2.f, g.uz, g.sz);
+                        g.ex = df_add(g.px, dt * g.ux); g.ey = df_add(g.py, dt * g.uy); g.ez = df_add(g.pz, dt * g.uz);
+                        g.ux = fmaf(dt, Fx, g.vx); g.uy = fmaf(dt, Fy, g.vy); g.uz = fmaf(dt, Fz, g.vz);
+                        g.phase = PH_EVAL3;
+                    } else {
+                        g.gx += Fx; g.gy += Fy; g.gz += Fz;
+                        g.esum += E;
+                        g.sx += g.ux; g.sy += g.uy; g.sz += g.uz;
+                        const float s6 = dt / 6.f;
+                        g.px = df_add(g.px, s6 * g.sx);
+                        g.py = df_add(g.py, s6 * g.sy);
+                        g.pz = df_add(g.pz, s6 * g.sz);
+                        g.vx = fmaf(s6, g.gx, g.vx); g.vy = fmaf(s6, g.gy, g.vy); g.vz = fmaf(s6, g.gz, g.vz);
+                        SFx = g.gx / 6.f; SFy = g.gy / 6.f; SFz = g.gz / 6.f;
+                        SE = g.esum / 6.0;
+                        step_done = true;
+                    }
+                }
+                if (step_done) {
+                    // checkConvergence (minimiser.cpp:15-37)
+                    const double ediff = SE - g.e_last;
+                    g.e_last = SE;
+                    const float fl = sqrtf(SFx * SFx + SFy * SFy + SFz * SFz);
+                    bool conv;
+                    if (P.minterm == MAFM_TERM_E) conv = fabs(ediff) < P.etol;
+                    else if (P.minterm == MAFM_TERM_F) conv = fl < (float)P.ftol;
+                    else conv = fabs(ediff) < P.etol && fl < (float)P.ftol;
+                    if (conv) {
+                        g.phase = PH_OUT;
+                    } else {
+                        if (P.minimiser == MAFM_MIN_SD) {
+                            const float sdt = (float)P.dt;
+                            g.px = df_add(g.px, sdt * SFx);
+                            g.py = df_add(g.py, sdt * SFy);
+                            g.pz = df_add(g.pz, sdt * SFz);
+                        } else {
+                            // FIRE velocity mixing and time-step control (minimiser.cpp:105-126)
+                            const float wx = g.vx, wy = g.vy, wz = g.vz;
+                            const float pw = wx * SFx + wy * SFy + wz * SFz;
+                            float hx2 = 0.f, hy2 = 0.f, hz2 = 0.f;
+                            if (fl > 1e-10f) {
+                                const float inv = 1.f / fl;
+                                hx2 = SFx * inv; hy2 = SFy * inv; hz2 = SFz * inv;
+                            }
+                            const float vl = sqrtf(wx * wx + wy * wy + wz * wz);
+                            const float a = g.alpha, b = 1.f - a;
+                            g.vx = b * wx + a * hx2 * vl;
+                            g.vy = b * wy + a * hy2 * vl;
+                            g.vz = b * wz + a * hz2 * vl;
+                            if (pw < 0.f) {
+                                g.vx = g.vy = g.vz = 0.f;
+                                g.nnn = 0;
+                                g.fdt *= 0.5f;
+                                g.alpha = 0.1f;
+                            } else {
+                                if (g.nnn > 5) {
+                                    g.fdt = fminf(g.fdt * 1.1f, (float)(10 * P.dt));
+                                    g.alpha *= 0.99f;
+                                }
+                                g.nnn++;
+                            }
+                        }
+                        g.n_tot++;
+                        g.phase = g.n_tot >= P.maxsteps ? PH_OUT : PH_EVAL0;
+                    }
+                    g.ex = g.px; g.ey = g.py; g.ez = g.pz;
+                }
+            }
+        }
+        __syncwarp();
+    }
+
+    // per-warp totals
+    for (int off = 16; off > 0; off >>= 1) {
+        my_steps += __shfl_xor_sync(kFull, my_steps, off);
+        my_evals += __shfl_xor_sync(kFull, my_evals, off);
+        my_pairs += __shfl_xor_sync(kFull, my_pairs, off);
+        status_or |= __shfl_xor_sync(kFull, status_or, off);
+        err |= __shfl_xor_sync(kFull, err, off);
+    }
+    if (lane == 0) {
+        atomicAdd(&ctr->total_steps, my_steps);
+        atomicAdd(&ctr->force_evals, my_evals);
+        atomicAdd(&ctr->pair_evals, my_pairs);
+        if (status_or | err) atomicOr(&ctr->error_word, status_or | err);
+    }
+}
+
+// ---------------------------------------------------------------- sample ----
+
+__global__ void sample32_kernel(const ScanParams p, int what, const double* pts, long long n,
+                                double* out, RunCounters* ctr) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    unsigned err = 0;
+    const DF x = df_split(pts[3 * i]), y = df_split(pts[3 * i + 1]), z = df_split(pts[3 * i + 2]);
+    Acc acc;
+    acc.zero();
+    int outside = 0;
+    if (what == 1) {
+        float v[4] = {0, 0, 0, 0};
+        if (p.es.g32) {
+            float qx, qy, qz;
+            rel_origin(p.es, x, y, z, qx, qy, qz);
+            interp32(p.es, qx, qy, qz, v, outside, err);
+        }
+        acc.add(v);
+    } else {
+        const bool coul = p.has_coulomb != 0;
+        for (int j0 = 0; j0 < p.n_terms_direct; j0 += kChunk) {
+            float v[4] = {0, 0, 0, 0};
+            for (int j = j0; j < min(j0 + kChunk, p.n_terms_direct); ++j) {
+                const AtomRec32 t = p.atoms32[j];
+                pair32(t, (x.hi - t.a.x) + x.lo, (y.hi - t.a.y) + y.lo, (z.hi - t.a.z) + z.lo, coul, v);
+            }
+            acc.add(v);
+        }
+        float v[4] = {0, 0, 0, 0};
+        if (p.ts_mode == 1) {
+            float qx, qy, qz;
+            rel_origin(p.es, x, y, z, qx, qy, qz);
+            interp32(p.es, qx, qy, qz, v, outside, err);
+        } else if (p.ts_mode == 2) {
+            float qx, qy, qz;
+            rel_origin(p.grid, x, y, z, qx, qy, qz);
+            interp32(p.grid, qx, qy, qz, v, outside, err);
+        }
+        acc.add(v);
+    }
+    for (int m = 0; m < 4; ++m) out[4 * i + m] = (double)acc.s[m] + (double)acc.c[m];
+    if (err) atomicOr(&ctr->error_word, err);
+}
+
+// ------------------------------------------------------------ grid build ----
+// Simulation::buildTipGridInteractions (simulation.cpp:420-501) in FP32:
+// one thread per node, terms staged through shared memory in tiles shared by
+// the whole block (all threads read the same term: broadcast).
+
+constexpr int kBuildTile = 2048;   // terms per shared-memory tile (64 KB)
+
+__global__ void __launch_bounds__(256) grid_build32_kernel(const ScanParams p, const GridView g,
+                                                           float4* out, RunCounters* ctr) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    AtomRec32* tile = reinterpret_cast<AtomRec32*>(smem_raw);
+    const long long total = (long long)g.n[0] * g.n[1] * g.n[2];
+    const int n = p.n_terms_direct;
+    const bool coul = p.has_coulomb != 0;
+    unsigned err = 0;
+    for (long long base = (long long)blockIdx.x * blockDim.x; base < total;
+         base += (long long)gridDim.x * blockDim.x) {
+        const long long idx = base + threadIdx.x;
+        const bool valid = idx < total;
+        DF tx{0, 0}, ty{0, 0}, tz{0, 0};
+        if (valid) {
+            const int k = (int)(idx % g.n[2]);
+            const long long ij = idx / g.n[2];
+            const int j = (int)(ij % g.n[1]), i = (int)(ij / g.n[1]);
+            double x, y;
+            dummy_xy(p, p.tip_pbc != 0, i * g.basis[0] + g.origin[0], j * g.basis[4] + g.origin[1], x, y);
+            tx = df_split(x);
+            ty = df_split(y);
+            tz = df_split(k * g.basis[8] + g.origin[2]);
+        }
+        Acc acc;
+        acc.zero();
+        for (int t0 = 0; t0 < n; t0 += kBuildTile) {
+            const int cnt = min(kBuildTile, n - t0);
+            __syncthreads();
+            for (int q = threadIdx.x; q < cnt; q += blockDim.x) tile[q] = p.atoms32[t0 + q];
+            __syncthreads();
+            for (int j0 = 0; j0 < cnt; j0 += kChunk) {
+                float v[4] = {0, 0, 0, 0};
+#pragma unroll
+                for (int u = 0; u < kChunk; ++u) {
+                    const int j = j0 + u;
+                    if (j < cnt) {
+                        const AtomRec32 t = tile[j];
+                        pair32(t, (tx.hi - t.a.x) + tx.lo, (ty.hi - t.a.y) + ty.lo,
+                               (tz.hi - t.a.z) + tz.lo, coul, v);
+                    }
+                }
+                acc.add(v);
+            }
+        }
+        if (valid) {
+            if (p.es.g32) {
+                float v[4] = {0, 0, 0, 0};
+                float qx, qy, qz;
+                rel_origin(p.es, tx, ty, tz, qx, qy, qz);
+                int unused = 0;
+                interp32(p.es, qx, qy, qz, v, unused, err);
+                acc.add(v);
+            }
+            out[idx] = make_float4(acc.s[0] + acc.c[0], acc.s[1] + acc.c[1], acc.s[2] + acc.c[2],
+                                   acc.s[3] + acc.c[3]);
+        }
+    }
+    if (err) atomicOr(&ctr->error_word, err);
+}
+
+template <int G>
+cudaError_t launch_g(const BatchScan* scans, int n_scans, long long n_tiles,
+                     const Relax32Config& cfg, RunCounters* ctr, cudaStream_t s) {
+    const size_t slice = sizeof(WarpHdr) + (size_t)cfg.smem_terms * sizeof(AtomRec32);
+    const size_t smem = slice * (size_t)(cfg.block / 32);
+    cudaError_t e = cudaFuncSetAttribute(relax32_kernel<G>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    int blocks = cfg.blocks;
+    if (blocks <= 0) {
+        int per_sm = 0;
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, relax32_kernel<G>, cfg.block, smem);
+        if (e != cudaSuccess) return e;
+        if (per_sm <= 0) return cudaErrorInvalidConfiguration;
+        blocks = sm_count() * per_sm;
+    }
+    // No more warps than tiles.
+    const long long warps_needed = n_tiles;
+    const long long max_blocks = (warps_needed + cfg.block / 32 - 1) / (cfg.block / 32);
+    if (blocks > max_blocks) blocks = (int)max_blocks;
+    if (blocks < 1) blocks = 1;
+    const unsigned long long watchdog_ns =
+        (unsigned long long)(cfg.watchdog_s > 0 ? cfg.watchdog_s : 600.0) * 1000000000ull;
+    relax32_kernel<G><<<blocks, cfg.block, smem, s>>>(scans, n_scans, n_tiles, cfg.cols_per_tile,
+                                                      cfg.smem_terms, watchdog_ns, ctr);
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+int sm_count() {
+    static int count = 0;
+    if (!count) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&count, cudaDevAttrMultiProcessorCount, dev);
+        if (count <= 0) count = 1;
+    }
+    return count;
+}
+
+cudaError_t launch_relax32(const BatchScan* scans_dev, int n_scans, long long n_tiles,
+                           const Relax32Config& cfg, RunCounters* ctr, cudaStream_t s) {
+    if (cfg.block % 32 != 0 || cfg.block < 32 || cfg.block > 256) return cudaErrorInvalidValue;
+    switch (cfg.lanes) {
+        case 1: return launch_g<1>(scans_dev, n_scans, n_tiles, cfg, ctr, s);
+        case 2: return launch_g<2>(scans_dev, n_scans, n_tiles, cfg, ctr, s);
+        case 4: return launch_g<4>(scans_dev, n_scans, n_tiles, cfg, ctr, s);
+        case 8: return launch_g<8>(scans_dev, n_scans, n_tiles, cfg, ctr, s);
+        case 16: return launch_g<16>(scans_dev, n_scans, n_tiles, cfg, ctr, s);
+        case 32: return launch_g<32>(scans_dev, n_scans, n_tiles, cfg, ctr, s);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+cudaError_t launch_sample32(const ScanParams& p, int what, const double* pts, int64_t n,
+                            double* out, RunCounters* ctr, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    sample32_kernel<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(p, what, pts, n, out, ctr);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_grid_build32(const ScanParams& p, const GridView& g, float4* out,
+                                RunCounters* ctr, cudaStream_t s) {
+    const size_t smem = (size_t)kBuildTile * sizeof(AtomRec32);
+    cudaError_t e = cudaFuncSetAttribute(grid_build32_kernel,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    const long long total = (long long)g.n[0] * g.n[1] * g.n[2];
+    long long blocks = (total + 255) / 256;
+    const long long cap = (long long)sm_count() * 8;
+    if (blocks > cap) blocks = cap;
+    if (blocks < 1) blocks = 1;
+    grid_build32_kernel<<<(unsigned)blocks, 256, smem, s>>>(p, g, out, ctr);
+    return cudaGetLastError();
+}
+
+}  // namespace mafm

@@ -1,0 +1,810 @@
+// scan.cu — device-resident scans and the relax / sample / grid entry points
+// of the C ABI.
+//
+//   mafm_scan_create   packs the tip–atom terms in the reference's interaction
+//                      order (simulation.cpp:238-320, 503-515), uploads them,
+//                      computes the external field by FFT on the GPU
+//                      (ElectrostaticPotentialInteraction ctor,
+//                      interactions.cpp:53-234, with cuFFT in FP64) and
+//                      records the rigid-grid geometry (simulation.cpp:428-441).
+//   rigid grids        are built on first use, FP64 for MAFM_FP64 runs and
+//                      FP32 for MAFM_FP32C runs (simulation.cpp:445-501).
+//   mafm_run           plain FP64 kernel or the FP32 persistent kernel.
+//   mafm_run_batch     many scans in one persistent FP32 launch.
+#include <cufft.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdlib>
+#include <cstring>
+#include <vector>
+
+#include "mafm_internal.h"
+
+namespace mafm {
+namespace {
+
+constexpr double kPi = 3.14159265358979323846;
+
+// Device buffer owned by a scan.
+template <class T>
+struct DevBuf {
+    T* p = nullptr;
+    size_t n = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf&) = delete;
+    DevBuf& operator=(const DevBuf&) = delete;
+    ~DevBuf() { release(); }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+    void alloc(size_t count) {
+        if (count <= n && p) return;
+        release();
+        if (count == 0) return;
+        cudaError_t e = cudaMalloc(&p, count * sizeof(T));
+        if (e != cudaSuccess) {
+            p = nullptr;
+            fail(MAFM_E_NOMEM, "cudaMalloc of %zu bytes failed: %s", count * sizeof(T),
+                 cudaGetErrorString(e));
+        }
+        n = count;
+    }
+};
+
+struct M3 {
+    double v[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+};
+
+double det3(const M3& m) {
+    double d = 0;
+    d = m.v[0][0] * (m.v[1][1] * m.v[2][2] - m.v[1][2] * m.v[2][1]);
+    d += m.v[0][1] * (m.v[1][2] * m.v[2][0] - m.v[1][0] * m.v[2][2]);
+    d += m.v[0][2] * (m.v[1][0] * m.v[2][1] - m.v[1][1] * m.v[2][0]);
+    return d;
+}
+
+// Matrix3::inverse (matrices.hpp:89-116)
+M3 inv3(const M3& m) {
+    M3 r;
+    const double inv_det = 1 / det3(m);
+    const double a = m.v[0][0], b = m.v[0][1], c = m.v[0][2];
+    const double d = m.v[1][0], e = m.v[1][1], f = m.v[1][2];
+    const double g = m.v[2][0], h = m.v[2][1], i = m.v[2][2];
+    r.v[0][0] = inv_det * (e * i - f * h);
+    r.v[0][1] = -inv_det * (b * i - c * h);
+    r.v[0][2] = inv_det * (b * f - c * e);
+    r.v[1][0] = -inv_det * (d * i - f * g);
+    r.v[1][1] = inv_det * (a * i - c * g);
+    r.v[1][2] = -inv_det * (a * f - c * d);
+    r.v[2][0] = inv_det * (d * h - e * g);
+    r.v[2][1] = -inv_det * (a * h - b * g);
+    r.v[2][2] = inv_det * (a * e - b * d);
+    return r;
+}
+
+bool is_diagonal(const M3& m) {   // Matrix3::isDiagonal (matrices.hpp:71-86)
+    double ds = 0, nd = 0;
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) {
+            if (i == j) ds += std::abs(m.v[i][i]);
+            else nd += std::abs(m.v[i][j]);
+        }
+    return nd < 1.0e-10 * ds;
+}
+
+M3 from_rowmajor(const double* a) {
+    M3 m;
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c) m.v[r][c] = a[3 * r + c];
+    return m;
+}
+
+void to_rowmajor(const M3& m, double* a) {
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c) a[3 * r + c] = m.v[r][c];
+}
+
+// ---- external field kernels (FP64) ----------------------------------------
+
+__global__ void real_to_complex(const double* v, cufftDoubleComplex* c, long long n) {
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x)
+        c[i] = make_cuDoubleComplex(v[i], 0.0);
+}
+
+// E(k) = V(k) * (vol * rho(k))  (interactions.cpp:139-146)
+__global__ void kspace_product(cufftDoubleComplex* V, const cufftDoubleComplex* R, double vol,
+                               long long n) {
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        const double ar = vol * R[i].x, ai = vol * R[i].y;
+        const double vr = V[i].x, vi = V[i].y;
+        V[i] = make_cuDoubleComplex(vr * ar - vi * ai, vr * ai + vi * ar);
+    }
+}
+
+struct KBasis {
+    double kb[9];   // reciprocal basis (B diag(n))^-1^T, row-major
+    int n[3];
+};
+
+// -2 pi i (ka + kb + kc)_comp E(k), Nyquist wrap at i >= n/2 (interactions.cpp:165-225)
+__global__ void gradient_mult(const cufftDoubleComplex* E, cufftDoubleComplex* out, KBasis K,
+                              int comp) {
+    const long long N = (long long)K.n[0] * K.n[1] * K.n[2];
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < N;
+         i += (long long)gridDim.x * blockDim.x) {
+        const int iz = (int)(i % K.n[2]);
+        const long long r = i / K.n[2];
+        const int iy = (int)(r % K.n[1]), ix = (int)(r / K.n[1]);
+        double ka = ix * K.kb[3 * comp + 0];
+        if (ix >= K.n[0] / 2) ka -= K.n[0] * K.kb[3 * comp + 0];
+        double kbv = iy * K.kb[3 * comp + 1];
+        if (iy >= K.n[1] / 2) kbv -= K.n[1] * K.kb[3 * comp + 1];
+        double kc = iz * K.kb[3 * comp + 2];
+        if (iz >= K.n[2] / 2) kc -= K.n[2] * K.kb[3 * comp + 2];
+        const double kk = ka + kbv + kc;
+        out[i] = make_cuDoubleComplex(2.0 * kPi * kk * E[i].y, -2.0 * kPi * kk * E[i].x);
+    }
+}
+
+// Real part / N into one component of the node array; imaginary residue check
+// of ffti_data_grid (fft.cpp:79-83): only positive residues are checked.
+__global__ void take_real(const cufftDoubleComplex* in, Node64* out, int comp, long long N,
+                          unsigned long long* max_bits) {
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < N;
+         i += (long long)gridDim.x * blockDim.x) {
+        const double v = in[i].x / N;
+        double* o = reinterpret_cast<double*>(out + i);
+        o[comp] = v;
+        const double im = in[i].y / N;
+        if (im > 1.0e-8) atomicMax(max_bits, (unsigned long long)__double_as_longlong(im));
+    }
+}
+
+__global__ void nodes_to_float4(const Node64* in, float4* out, long long n) {
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        const Node64 v = in[i];
+        out[i] = make_float4((float)v.x, (float)v.y, (float)v.z, (float)v.w);
+    }
+}
+
+__global__ void write_batch(BatchScan* dst, BatchScan v) { *dst = v; }
+
+unsigned grid_blocks(long long n) {
+    long long b = (n + 255) / 256;
+    const long long cap = (long long)sm_count() * 32;
+    return (unsigned)std::max(1ll, std::min(b, cap));
+}
+
+}  // namespace
+}  // namespace mafm
+
+struct mafm_scan {
+    int device = 0;
+    mafm_scan_desc d{};                 // scalars of the descriptor (pointers not kept)
+    mafm::ScanParams P{};               // shared parameters; pointers filled per precision
+    mafm::DevBuf<mafm::AtomRec64> atoms64;
+    mafm::DevBuf<mafm::AtomRec32> atoms32;
+    mafm::DevBuf<mafm::Node64> es64, grid64;
+    mafm::DevBuf<float4> es32, grid32;
+    mafm::GridView es_view{}, grid_view{};
+    bool grid64_built = false, grid32_built = false;
+    mafm::DevBuf<mafm::RunCounters> ctr;
+    mafm::DevBuf<mafm::BatchScan> batch;
+    mafm::DevBuf<mafm_point> stage;
+    mafm::RunCounters* host_ctr = nullptr;   // pinned
+    int n_pairs_per_eval = 0;
+    int has_coulomb = 0;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    ~mafm_scan() {
+        if (host_ctr) cudaFreeHost(host_ctr);
+        if (ev0) cudaEventDestroy(ev0);
+        if (ev1) cudaEventDestroy(ev1);
+    }
+};
+
+namespace mafm {
+namespace {
+
+void validate(const mafm_scan_desc* d) {
+    if (!d) fail(MAFM_E_INVALID, "null descriptor");
+    if (d->n_atoms < 0 || d->n_types < 0) fail(MAFM_E_INVALID, "negative atom or type count");
+    if (d->n_atoms > 0 && (!d->pos || !d->type || !d->tip_pair))
+        fail(MAFM_E_INVALID, "descriptor has atoms but null pos/type/tip_pair");
+    if (d->n_atoms > 0 && d->coulomb && !d->charge)
+        fail(MAFM_E_INVALID, "coulomb on but charge is null");
+    for (int a = 0; a < d->n_atoms; ++a)
+        if (d->type[a] < 0 || d->type[a] >= d->n_types)
+            fail(MAFM_E_INVALID, "atom %d has type index %d outside [0, %d)", a, d->type[a], d->n_types);
+    for (int t = 0; t < d->n_types; ++t)
+        if (d->tip_pair[t].kind != MAFM_PAIR_LJ && d->tip_pair[t].kind != MAFM_PAIR_MORSE)
+            fail(MAFM_E_INVALID, "pair kind %d of type %d", d->tip_pair[t].kind, t);
+    if (d->dummy_pair.kind != MAFM_PAIR_LJ && d->dummy_pair.kind != MAFM_PAIR_MORSE)
+        fail(MAFM_E_INVALID, "dummy pair kind %d", d->dummy_pair.kind);
+    if (d->nx < 1 || d->ny < 1 || d->nz < 1) fail(MAFM_E_INVALID, "empty scan grid %d x %d x %d", d->nx, d->ny, d->nz);
+    if ((long long)d->nx * d->ny > 0x7fffffffll) fail(MAFM_E_RANGE, "more than 2^31 pixel columns");
+    if (d->minimiser != MAFM_MIN_SD && d->minimiser != MAFM_MIN_FIRE) fail(MAFM_E_INVALID, "minimiser %d", d->minimiser);
+    if (d->integrator < MAFM_INT_EULER || d->integrator > MAFM_INT_RK4) fail(MAFM_E_INVALID, "integrator %d", d->integrator);
+    if (d->minterm < MAFM_TERM_E || d->minterm > MAFM_TERM_EF) fail(MAFM_E_INVALID, "minterm %d", d->minterm);
+    if (d->use_external_potential) {
+        if (!d->epot) fail(MAFM_E_INVALID, "external potential on but epot is null");
+        if (d->epot_n[0] < 1 || d->epot_n[1] < 1 || d->epot_n[2] < 1) fail(MAFM_E_INVALID, "empty potential grid");
+    }
+}
+
+// Tip–atom terms in the reference's interaction order.
+void pack_terms(mafm_scan& s, const mafm_scan_desc& d) {
+    const M3 cell = from_rowmajor(d.cell);
+    std::vector<AtomRec64> t64;
+    const int images = d.vdw_pbc ? 9 : 1;
+    t64.reserve((size_t)d.n_atoms * images);
+    for (int ia = -1; ia <= 1; ++ia)
+        for (int ib = -1; ib <= 1; ++ib) {
+            if (!d.vdw_pbc && (ia != 0 || ib != 0)) continue;
+            double sx = 0, sy = 0, sz = 0;
+            if (d.vdw_pbc) {   // simulation.cpp:303-306
+                sx = ia * cell.v[0][0] + ib * cell.v[0][1];
+                sy = ia * cell.v[1][0] + ib * cell.v[1][1];
+                sz = ia * cell.v[2][0] + ib * cell.v[2][1];
+            }
+            for (int a = 0; a < d.n_atoms; ++a) {
+                const mafm_pair& p = d.tip_pair[d.type[a]];
+                AtomRec64 r{};
+                if (d.vdw_pbc) {
+                    r.x = d.pos[3 * a] + sx;
+                    r.y = d.pos[3 * a + 1] + sy;
+                    r.z = d.pos[3 * a + 2] + sz;
+                } else {
+                    r.x = d.pos[3 * a];
+                    r.y = d.pos[3 * a + 1];
+                    r.z = d.pos[3 * a + 2];
+                }
+                r.kind = p.kind;
+                r.p0 = p.p[0];
+                r.p1 = p.p[1];
+                r.p2 = p.p[2];
+                // addCoulombInteraction (simulation.cpp:269-295): only without
+                // vdw_pbc, and only if both charges are non-zero.
+                r.coul = d.coulomb && !d.vdw_pbc && d.tip_charge != 0 && d.charge[a] != 0;
+                r.qq = r.coul ? d.qbase * d.tip_charge * d.charge[a] : 0.0;
+                t64.push_back(r);
+            }
+        }
+    // FP32 copy, LJ terms first so that lanes sharing a column rarely diverge on the kind.
+    std::vector<AtomRec32> t32;
+    t32.reserve(t64.size());
+    int n_coul = 0;
+    for (int pass = 0; pass < 2; ++pass)
+        for (const AtomRec64& r : t64) {
+            if ((pass == 0) != (r.kind == MAFM_PAIR_LJ)) continue;
+            AtomRec32 q;
+            q.a = make_float4((float)r.x, (float)r.y, (float)r.z, (float)r.qq);
+            int kind = r.kind;
+            float kf;
+            std::memcpy(&kf, &kind, sizeof kf);
+            q.b = make_float4((float)r.p0, (float)r.p1, (float)r.p2, kf);
+            t32.push_back(q);
+            n_coul += r.coul;
+        }
+    s.atoms64.alloc(std::max<size_t>(t64.size(), 1));
+    s.atoms32.alloc(std::max<size_t>(t32.size(), 1));
+    if (!t64.empty()) {
+        cuda_check(cudaMemcpy(s.atoms64.p, t64.data(), t64.size() * sizeof(AtomRec64),
+                              cudaMemcpyHostToDevice), "upload terms");
+        cuda_check(cudaMemcpy(s.atoms32.p, t32.data(), t32.size() * sizeof(AtomRec32),
+                              cudaMemcpyHostToDevice), "upload terms");
+    }
+    s.P.n_terms = (int)t64.size();
+    s.P.n_terms_direct = d.rigidgrid ? 0 : s.P.n_terms;
+    s.has_coulomb = n_coul > 0;
+    s.P.has_coulomb = s.has_coulomb;
+    s.n_pairs_per_eval = d.rigidgrid ? 0 : (int)t64.size() + n_coul;
+}
+
+// ElectrostaticPotentialInteraction ctor (interactions.cpp:53-234) on the GPU.
+void build_external_field(mafm_scan& s, const mafm_scan_desc& d) {
+    const int n0 = d.epot_n[0], n1 = d.epot_n[1], n2 = d.epot_n[2];
+    const long long N = (long long)n0 * n1 * n2;
+    const M3 B = from_rowmajor(d.epot_basis);
+    const bool orth = is_diagonal(B);
+    // Gaussian tip charge on the host, in the reference's order (interactions.cpp:63-105).
+    std::vector<double> rho((size_t)N, 0.0);
+    {
+        const double w = 0.5;   // g_tip_gaussian_width (globals.hpp:17)
+        const double w2 = pow(w, 2);
+        const double norm = 1.0 / pow(w * sqrt(2.0 * kPi), 3);
+        const int nmin = std::min(std::min(n0, n1), n2);
+        int cut[3] = {nmin, nmin, nmin};
+        for (int a = 0; a < 3; ++a)
+            for (int i = 0; i < nmin - 1; i++) {
+                const double vx = i * B.v[0][a], vy = i * B.v[1][a], vz = i * B.v[2][a];
+                const double sq = vx * vx + vy * vy + vz * vz;
+                if (exp(-0.5 * sq / w2) < 1.0e-10) {   // g_gaussian_cutoff_value
+                    cut[a] = i;
+                    break;
+                }
+            }
+        const int n[3] = {n0, n1, n2};
+        for (int ix = -cut[0]; ix <= cut[0]; ix++)
+            for (int iy = -cut[1]; iy <= cut[1]; iy++)
+                for (int iz = -cut[2]; iz < cut[2]; iz++) {
+                    double px, py, pz;
+                    if (orth) {
+                        px = 0 + ix * B.v[0][0];
+                        py = 0 + iy * B.v[1][1];
+                        pz = 0 + iz * B.v[2][2];
+                    } else {
+                        px = 0 + (B.v[0][0] * ix + B.v[0][1] * iy + B.v[0][2] * iz);
+                        py = 0 + (B.v[1][0] * ix + B.v[1][1] * iy + B.v[1][2] * iz);
+                        pz = 0 + (B.v[2][0] * ix + B.v[2][1] * iy + B.v[2][2] * iz);
+                    }
+                    const double r2 = px * px + py * py + pz * pz;
+                    int g[3] = {ix, iy, iz};
+                    for (int a = 0; a < 3; ++a)
+                        if (g[a] < 0 || g[a] >= n[a]) {
+                            const int k = (int)floor((double)g[a] / n[a]);
+                            g[a] -= k * n[a];
+                        }
+                    rho[((size_t)g[0] * n1 + g[1]) * n2 + g[2]] +=
+                        d.tip_charge * norm * exp(-0.5 * r2 / w2);
+                }
+    }
+    DevBuf<double> real;
+    DevBuf<cufftDoubleComplex> V, R;
+    real.alloc((size_t)N);
+    V.alloc((size_t)N);
+    R.alloc((size_t)N);
+    const unsigned nb = grid_blocks(N);
+    cuda_check(cudaMemcpy(real.p, d.epot, N * sizeof(double), cudaMemcpyHostToDevice), "upload potential");
+    real_to_complex<<<nb, 256>>>(real.p, V.p, N);
+    cuda_check(cudaMemcpy(real.p, rho.data(), N * sizeof(double), cudaMemcpyHostToDevice), "upload rho");
+    real_to_complex<<<nb, 256>>>(real.p, R.p, N);
+    cuda_check(cudaGetLastError(), "external field setup");
+    real.release();
+    cufftHandle plan;
+    if (cufftPlan3d(&plan, n0, n1, n2, CUFFT_Z2Z) != CUFFT_SUCCESS)
+        fail(MAFM_E_CUDA, "cufftPlan3d(%d, %d, %d) failed", n0, n1, n2);
+    struct PlanGuard { cufftHandle h; ~PlanGuard() { cufftDestroy(h); } } guard{plan};
+    if (cufftExecZ2Z(plan, V.p, V.p, CUFFT_FORWARD) != CUFFT_SUCCESS ||
+        cufftExecZ2Z(plan, R.p, R.p, CUFFT_FORWARD) != CUFFT_SUCCESS)
+        fail(MAFM_E_CUDA, "forward FFT of the external potential failed");
+    kspace_product<<<nb, 256>>>(V.p, R.p, det3(B), N);
+    // reciprocal basis (fft.cpp:41-47)
+    M3 bn;
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c) bn.v[r][c] = B.v[r][c] * d.epot_n[c];
+    const M3 bi = inv3(bn);
+    KBasis K;
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c) K.kb[3 * r + c] = bi.v[c][r];
+    K.n[0] = n0; K.n[1] = n1; K.n[2] = n2;
+    s.es64.alloc((size_t)N);
+    DevBuf<unsigned long long> maxbits;
+    maxbits.alloc(1);
+    cuda_check(cudaMemset(maxbits.p, 0, sizeof(unsigned long long)), "memset");
+    for (int comp = -1; comp < 3; ++comp) {
+        if (comp < 0) cuda_check(cudaMemcpy(R.p, V.p, N * sizeof(cufftDoubleComplex), cudaMemcpyDeviceToDevice), "copy");
+        else gradient_mult<<<nb, 256>>>(V.p, R.p, K, comp);
+        if (cufftExecZ2Z(plan, R.p, R.p, CUFFT_INVERSE) != CUFFT_SUCCESS)
+            fail(MAFM_E_CUDA, "inverse FFT of the external field failed");
+        take_real<<<nb, 256>>>(R.p, s.es64.p, comp < 0 ? 3 : comp, N, maxbits.p);
+    }
+    s.es32.alloc((size_t)N);
+    nodes_to_float4<<<nb, 256>>>(s.es64.p, s.es32.p, N);
+    cuda_check(cudaDeviceSynchronize(), "external field");
+    unsigned long long bits = 0;
+    cuda_check(cudaMemcpy(&bits, maxbits.p, sizeof bits, cudaMemcpyDeviceToHost), "readback");
+    if (bits) {
+        double im;
+        std::memcpy(&im, &bits, sizeof im);
+        fail(MAFM_E_RANGE, "Imaginary part of inverse FFT exceeded threshold 1.0e-8! Value: %e",
+             im * (double)N);
+    }
+    GridView& g = s.es_view;
+    g.g64 = s.es64.p;
+    g.g32 = s.es32.p;
+    g.n[0] = n0; g.n[1] = n1; g.n[2] = n2;
+    g.periodic = 1;
+    g.orthogonal = orth;
+    to_rowmajor(B, g.basis);
+    to_rowmajor(inv3(B), g.inv);
+    for (int a = 0; a < 3; ++a) g.origin[a] = d.epot_origin[a];
+}
+
+// Geometry of the rigid grid (simulation.cpp:428-441).
+void rigid_grid_geometry(mafm_scan& s, const mafm_scan_desc& d) {
+    GridView& g = s.grid_view;
+    const double sp[3] = {d.dx / 2, d.dy / 2, d.dz / 2};
+    int border[3];
+    for (int a = 0; a < 3; ++a) border[a] = (int)ceil(1.5 / sp[a]);   // g_force_grid_margin
+    const double nx = floor(d.area[0] / sp[0]) + 2 * border[0] + 1;
+    const double ny = floor(d.area[1] / sp[1]) + 2 * border[1] + 1;
+    const double nz = floor((d.zhigh - d.zlow) / sp[2]) + 2 * border[2] + 1;
+    if (nx * ny * nz > 4.0e9) fail(MAFM_E_RANGE, "rigid grid of %.0f nodes is too large", nx * ny * nz);
+    g.n[0] = (int)nx;
+    g.n[1] = (int)ny;
+    g.n[2] = (int)nz;
+    g.origin[0] = -border[0] * sp[0];
+    g.origin[1] = -border[1] * sp[1];
+    g.origin[2] = d.zlow - d.tip_dummy_d - border[2] * sp[2];
+    std::memset(g.basis, 0, sizeof g.basis);
+    std::memset(g.inv, 0, sizeof g.inv);
+    for (int a = 0; a < 3; ++a) {
+        g.basis[4 * a] = sp[a];
+        g.inv[4 * a] = 1 / sp[a];
+    }
+    g.periodic = 0;
+    g.orthogonal = 1;
+}
+
+ScanParams build_params(const mafm_scan& s) {
+    ScanParams p = s.P;
+    p.n_terms_direct = s.d.rigidgrid ? 0 : p.n_terms;
+    return p;
+}
+
+// Parameters of the grid build: every tip–surface term plus the external field.
+ScanParams build_grid_params(const mafm_scan& s) {
+    ScanParams p = s.P;
+    p.n_terms_direct = p.n_terms;
+    p.ts_mode = s.d.use_external_potential ? 1 : 0;
+    p.es = s.es_view;
+    return p;
+}
+
+void zero_counters(mafm_scan& s, cudaStream_t st) {
+    cuda_check(cudaMemsetAsync(s.ctr.p, 0, sizeof(RunCounters), st), "reset counters");
+}
+
+void ensure_grid(mafm_scan& s, bool fp64, cudaStream_t st) {
+    if (!s.d.rigidgrid) return;
+    const long long N = (long long)s.grid_view.n[0] * s.grid_view.n[1] * s.grid_view.n[2];
+    if (fp64 && !s.grid64_built) {
+        s.grid64.alloc((size_t)N);
+        zero_counters(s, st);
+        cuda_check(launch_grid_build64(build_grid_params(s), s.grid_view, s.grid64.p, s.ctr.p, st), "grid build");
+        s.grid_view.g64 = s.grid64.p;
+        s.grid64_built = true;
+    }
+    if (!fp64 && !s.grid32_built) {
+        s.grid32.alloc((size_t)N);
+        zero_counters(s, st);
+        cuda_check(launch_grid_build32(build_grid_params(s), s.grid_view, s.grid32.p, s.ctr.p, st), "grid build");
+        s.grid_view.g32 = s.grid32.p;
+        s.grid32_built = true;
+    }
+    s.P.grid = s.grid_view;
+}
+
+bool is_device_ptr(const void* p) {
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+void check_device_errors(const RunCounters& c) {
+    if (c.error_word & ERR_GRID_INDEX)
+        fail(MAFM_E_RANGE, "Invalid grid point: the tip left the rigid force grid "
+                           "(force_grid.cpp:236-240 stops the reference here)");
+    if (c.error_word & ERR_STAGE_TIMEOUT)
+        fail(MAFM_E_DEVICE, "a bounded wait on the term staging barrier expired");
+    if (c.error_word & ERR_WATCHDOG)
+        fail(MAFM_E_DEVICE, "the relax kernel stopped at its watchdog time limit");
+}
+
+// Default FP32 launch shape: enough lanes per column that every SM gets work
+// several times over, one column per group per tile.
+Relax32Config default_config(long long n_cols, int max_terms, const mafm_run_opts* o) {
+    Relax32Config c{};
+    c.block = (o && o->block_threads) ? o->block_threads : 256;
+    const long long lanes_cap = (long long)sm_count() * 512;
+    int G = 1;
+    while (G < 32 && n_cols * G < 4 * lanes_cap) G *= 2;
+    if (max_terms <= 1) G = 1;
+    c.lanes = (o && o->lanes_per_column) ? o->lanes_per_column : G;
+    c.cols_per_tile = (o && o->columns_per_tile) ? o->columns_per_tile : 32 / c.lanes;
+    c.smem_terms = std::min(std::max(max_terms, 1), 256);
+    c.smem_terms = (c.smem_terms + 1) & ~1;
+    c.blocks = 0;
+    // Persistent-kernel time limit; MAFM_WATCHDOG_S overrides the 120 s default.
+    const char* w = getenv("MAFM_WATCHDOG_S");
+    c.watchdog_s = w ? atof(w) : 120.0;
+    return c;
+}
+
+}  // namespace
+}  // namespace mafm
+
+using namespace mafm;
+
+extern "C" {
+
+int mafm_scan_create(int device, const mafm_scan_desc* desc, mafm_scan** out) {
+    return guarded([&] {
+        if (!out) fail(MAFM_E_INVALID, "null output handle");
+        *out = nullptr;
+        validate(desc);
+        if (device >= 0) cuda_check(cudaSetDevice(device), "cudaSetDevice");
+        auto* s = new mafm_scan();
+        try {
+            cuda_check(cudaGetDevice(&s->device), "cudaGetDevice");
+            const mafm_scan_desc& d = *desc;
+            s->d = d;
+            s->d.pos = nullptr;
+            s->d.charge = nullptr;
+            s->d.type = nullptr;
+            s->d.tip_pair = nullptr;
+            s->d.epot = nullptr;
+            ScanParams& P = s->P;
+            std::memset(&P, 0, sizeof P);
+            pack_terms(*s, d);
+            P.atoms64 = s->atoms64.p;
+            P.atoms32 = s->atoms32.p;
+            P.ts_mode = d.rigidgrid ? 2 : (d.use_external_potential ? 1 : 0);
+            P.td_kind = d.dummy_pair.kind;
+            for (int k = 0; k < 3; ++k) P.td_p[k] = d.dummy_pair.p[k];
+            P.td_coul = d.tip_dummy_coulomb && d.dummy_charge != 0 && d.tip_charge != 0;
+            P.td_qq = P.td_coul ? d.qbase * d.dummy_charge * d.tip_charge : 0.0;
+            P.harm_k = d.harm_k;
+            P.harm_r0 = d.harm_r0;
+            P.tip_dummy_d = d.tip_dummy_d;
+            P.nx = d.nx; P.ny = d.ny; P.nz = d.nz;
+            P.tip_pbc = d.tip_pbc;
+            P.dx = d.dx; P.dy = d.dy; P.dz = d.dz; P.zhigh = d.zhigh;
+            std::memcpy(P.cell, d.cell, sizeof P.cell);
+            if (d.tip_pbc) to_rowmajor(inv3(from_rowmajor(d.cell)), P.cell_inv);
+            std::memcpy(P.offset, d.offset, sizeof P.offset);
+            P.minimiser = d.minimiser;
+            P.integrator = d.integrator;
+            P.minterm = d.minterm;
+            P.maxsteps = d.maxsteps;
+            P.etol = d.etol; P.ftol = d.ftol; P.dt = d.dt;
+            if (d.use_external_potential) build_external_field(*s, d);
+            P.es = s->es_view;
+            if (d.rigidgrid) rigid_grid_geometry(*s, d);
+            P.grid = s->grid_view;
+            s->ctr.alloc(1);
+            s->batch.alloc(1);
+            cuda_check(cudaMallocHost(&s->host_ctr, sizeof(RunCounters)), "cudaMallocHost");
+            cuda_check(cudaEventCreate(&s->ev0), "cudaEventCreate");
+            cuda_check(cudaEventCreate(&s->ev1), "cudaEventCreate");
+        } catch (...) {
+            delete s;
+            throw;
+        }
+        *out = s;
+    });
+}
+
+int mafm_scan_destroy(mafm_scan* scan) {
+    if (scan) {
+        cudaSetDevice(scan->device);
+        delete scan;
+    }
+    return MAFM_OK;
+}
+
+int mafm_scan_size(const mafm_scan* scan, int64_t* n_points, int64_t* n_columns) {
+    return guarded([&] {
+        if (!scan) fail(MAFM_E_INVALID, "null scan");
+        const int64_t cols = (int64_t)scan->d.nx * scan->d.ny;
+        if (n_columns) *n_columns = cols;
+        if (n_points) *n_points = cols * scan->d.nz;
+    });
+}
+
+int mafm_run(mafm_scan* scan, const mafm_run_opts* opts, mafm_point* out, mafm_run_stats* stats,
+             void* stream) {
+    return guarded([&] {
+        if (!scan || !out) fail(MAFM_E_INVALID, "null scan or output");
+        cuda_check(cudaSetDevice(scan->device), "cudaSetDevice");
+        cudaStream_t st = (cudaStream_t)stream;
+        const long long n_cols_all = (long long)scan->d.nx * scan->d.ny;
+        int cb = 0, ce = (int)n_cols_all;
+        if (opts && (opts->col_begin || opts->col_end)) {
+            cb = opts->col_begin;
+            ce = opts->col_end;
+            if (cb < 0 || ce > n_cols_all || cb > ce)
+                fail(MAFM_E_INVALID, "column range [%d, %d) outside [0, %lld)", cb, ce, n_cols_all);
+        }
+        const int prec = opts ? opts->precision : MAFM_FP64;
+        if (prec != MAFM_FP64 && prec != MAFM_FP32C) fail(MAFM_E_INVALID, "precision %d", prec);
+        const size_t n_pts = (size_t)(ce - cb) * scan->d.nz;
+        if (n_pts == 0) {
+            if (stats) *stats = mafm_run_stats{};
+            return;
+        }
+        const bool host_out = !is_device_ptr(out);
+        mafm_point* dout = out;
+        if (host_out) {
+            scan->stage.alloc(n_pts);
+            dout = scan->stage.p;
+        }
+        ensure_grid(*scan, prec == MAFM_FP64, st);
+        zero_counters(*scan, st);
+        cuda_check(cudaEventRecord(scan->ev0, st), "cudaEventRecord");
+        if (prec == MAFM_FP64) {
+            ScanParams p = build_params(*scan);
+            cuda_check(launch_relax64(p, dout, scan->ctr.p, cb, ce, st), "relax64 launch");
+        } else {
+            BatchScan b{};
+            b.p = build_params(*scan);
+            b.out = dout;
+            b.tile_begin = 0;
+            b.col_begin = cb;
+            b.col_end = ce;
+            b.n_pairs_per_eval = scan->n_pairs_per_eval;
+            b.has_coulomb = scan->has_coulomb;
+            write_batch<<<1, 1, 0, st>>>(scan->batch.p, b);
+            const Relax32Config cfg = default_config(ce - cb, b.p.n_terms_direct, opts);
+            const long long n_tiles = ((long long)(ce - cb) + cfg.cols_per_tile - 1) / cfg.cols_per_tile;
+            cuda_check(launch_relax32(scan->batch.p, 1, n_tiles, cfg, scan->ctr.p, st), "relax32 launch");
+        }
+        cuda_check(cudaEventRecord(scan->ev1, st), "cudaEventRecord");
+        if (host_out)
+            cuda_check(cudaMemcpyAsync(out, dout, n_pts * sizeof(mafm_point), cudaMemcpyDeviceToHost, st),
+                       "copy points to host");
+        if (stats || host_out) {
+            cuda_check(cudaMemcpyAsync(scan->host_ctr, scan->ctr.p, sizeof(RunCounters),
+                                       cudaMemcpyDeviceToHost, st), "copy counters");
+            cuda_check(cudaStreamSynchronize(st), "relax");
+            const RunCounters c = *scan->host_ctr;
+            if (stats) {
+                float ms = 0.f;
+                cudaEventElapsedTime(&ms, scan->ev0, scan->ev1);
+                stats->total_steps = c.total_steps;
+                stats->force_evals = c.force_evals;
+                stats->pair_evals = c.pair_evals;
+                stats->error_word = c.error_word;
+                stats->reserved = 0;
+                stats->kernel_ms = ms;
+            }
+            check_device_errors(c);
+        }
+    });
+}
+
+int mafm_run_batch(mafm_scan* const* scans, int32_t n_scans, const mafm_run_opts* opts,
+                   mafm_point* const* outs, mafm_run_stats* stats, void* stream) {
+    return guarded([&] {
+        if (!scans || !outs || n_scans <= 0) fail(MAFM_E_INVALID, "empty batch");
+        if (opts && opts->precision != MAFM_FP32C)
+            fail(MAFM_E_UNSUPPORTED, "batched runs use MAFM_FP32C");
+        if (opts && (opts->col_begin || opts->col_end))
+            fail(MAFM_E_INVALID, "column ranges are per scan; batches relax whole scans");
+        cudaStream_t st = (cudaStream_t)stream;
+        mafm_scan* s0 = scans[0];
+        if (!s0) fail(MAFM_E_INVALID, "null scan in batch");
+        cuda_check(cudaSetDevice(s0->device), "cudaSetDevice");
+        const bool host_out = !is_device_ptr(outs[0]);
+        std::vector<BatchScan> bs((size_t)n_scans);
+        std::vector<size_t> offsets((size_t)n_scans);
+        size_t total_pts = 0;
+        long long max_cols = 0, total_cols = 0;
+        int max_terms = 0;
+        for (int i = 0; i < n_scans; ++i) {
+            mafm_scan* s = scans[i];
+            if (!s || !outs[i]) fail(MAFM_E_INVALID, "null scan or output %d in batch", i);
+            if (s->device != s0->device) fail(MAFM_E_INVALID, "scans of one batch must share a device");
+            if (is_device_ptr(outs[i]) == host_out) fail(MAFM_E_INVALID, "batch outputs mix host and device memory");
+            offsets[i] = total_pts;
+            const long long cols = (long long)s->d.nx * s->d.ny;
+            total_pts += (size_t)cols * s->d.nz;
+            max_cols = std::max(max_cols, cols);
+            total_cols += cols;
+            ensure_grid(*s, false, st);
+            max_terms = std::max(max_terms, s->d.rigidgrid ? 0 : s->P.n_terms);
+        }
+        Relax32Config cfg = default_config(total_cols, max_terms, opts);
+        long long tiles = 0;
+        if (host_out) s0->stage.alloc(total_pts);
+        for (int i = 0; i < n_scans; ++i) {
+            mafm_scan* s = scans[i];
+            BatchScan& b = bs[i];
+            b.p = build_params(*s);
+            b.out = host_out ? s0->stage.p + offsets[i] : outs[i];
+            b.tile_begin = tiles;
+            b.col_begin = 0;
+            b.col_end = s->d.nx * s->d.ny;
+            b.n_pairs_per_eval = s->n_pairs_per_eval;
+            b.has_coulomb = s->has_coulomb;
+            tiles += ((long long)b.col_end + cfg.cols_per_tile - 1) / cfg.cols_per_tile;
+        }
+        DevBuf<BatchScan> dbs;
+        dbs.alloc(bs.size());
+        cuda_check(cudaMemcpyAsync(dbs.p, bs.data(), bs.size() * sizeof(BatchScan), cudaMemcpyHostToDevice, st),
+                   "upload batch");
+        zero_counters(*s0, st);
+        cuda_check(cudaEventRecord(s0->ev0, st), "cudaEventRecord");
+        cuda_check(launch_relax32(dbs.p, n_scans, tiles, cfg, s0->ctr.p, st), "relax32 batch launch");
+        cuda_check(cudaEventRecord(s0->ev1, st), "cudaEventRecord");
+        if (host_out)
+            for (int i = 0; i < n_scans; ++i) {
+                const size_t np = (size_t)scans[i]->d.nx * scans[i]->d.ny * scans[i]->d.nz;
+                cuda_check(cudaMemcpyAsync(outs[i], s0->stage.p + offsets[i], np * sizeof(mafm_point),
+                                           cudaMemcpyDeviceToHost, st), "copy points to host");
+            }
+        cuda_check(cudaMemcpyAsync(s0->host_ctr, s0->ctr.p, sizeof(RunCounters), cudaMemcpyDeviceToHost, st),
+                   "copy counters");
+        cuda_check(cudaStreamSynchronize(st), "batch relax");
+        const RunCounters c = *s0->host_ctr;
+        if (stats) {
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, s0->ev0, s0->ev1);
+            stats->total_steps = c.total_steps;
+            stats->force_evals = c.force_evals;
+            stats->pair_evals = c.pair_evals;
+            stats->error_word = c.error_word;
+            stats->reserved = 0;
+            stats->kernel_ms = ms;
+        }
+        check_device_errors(c);
+    });
+}
+
+int mafm_scan_sample(mafm_scan* scan, int32_t precision, int32_t what, const double* pts,
+                     int64_t n, double* out) {
+    return guarded([&] {
+        if (!scan || (n > 0 && (!pts || !out))) fail(MAFM_E_INVALID, "null argument");
+        if (n <= 0) return;
+        cuda_check(cudaSetDevice(scan->device), "cudaSetDevice");
+        const bool fp64 = precision == MAFM_FP64;
+        ensure_grid(*scan, fp64, nullptr);
+        DevBuf<double> dp, dout;
+        dp.alloc((size_t)n * 3);
+        dout.alloc((size_t)n * 4);
+        cuda_check(cudaMemcpy(dp.p, pts, (size_t)n * 3 * sizeof(double), cudaMemcpyHostToDevice), "upload points");
+        zero_counters(*scan, nullptr);
+        ScanParams p = build_params(*scan);
+        if (fp64) cuda_check(launch_sample64(p, what, dp.p, n, dout.p, scan->ctr.p, nullptr), "sample");
+        else cuda_check(launch_sample32(p, what, dp.p, n, dout.p, scan->ctr.p, nullptr), "sample");
+        cuda_check(cudaMemcpy(out, dout.p, (size_t)n * 4 * sizeof(double), cudaMemcpyDeviceToHost), "download");
+    });
+}
+
+int mafm_scan_grid_info(const mafm_scan* scan, int32_t what, int32_t n[3], double basis[9],
+                        double origin[3]) {
+    return guarded([&] {
+        if (!scan) fail(MAFM_E_INVALID, "null scan");
+        const GridView& g = what == 1 ? scan->es_view : scan->grid_view;
+        if ((what == 1 && !scan->d.use_external_potential) || (what != 1 && !scan->d.rigidgrid))
+            fail(MAFM_E_INVALID, "the scan has no such grid");
+        for (int a = 0; a < 3; ++a) {
+            if (n) n[a] = g.n[a];
+            if (origin) origin[a] = g.origin[a];
+        }
+        if (basis) std::memcpy(basis, g.basis, sizeof g.basis);
+    });
+}
+
+int mafm_scan_grid_copy(const mafm_scan* scan, int32_t what, double* out) {
+    return guarded([&] {
+        if (!scan || !out) fail(MAFM_E_INVALID, "null argument");
+        mafm_scan* s = const_cast<mafm_scan*>(scan);
+        cuda_check(cudaSetDevice(s->device), "cudaSetDevice");
+        const GridView* g;
+        const Node64* src;
+        if (what == 1) {
+            if (!s->d.use_external_potential) fail(MAFM_E_INVALID, "the scan has no external field");
+            g = &s->es_view;
+            src = s->es64.p;
+        } else {
+            if (!s->d.rigidgrid) fail(MAFM_E_INVALID, "the scan has no rigid grid");
+            ensure_grid(*s, true, nullptr);
+            g = &s->grid_view;
+            src = s->grid64.p;
+        }
+        const size_t N = (size_t)g->n[0] * g->n[1] * g->n[2];
+        cuda_check(cudaMemcpy(out, src, N * sizeof(Node64), cudaMemcpyDeviceToHost), "download grid");
+    });
+}
+
+}  // extern "C"

@@ -337,7 +337,7 @@ static int fire(Ctx* c, State* s) {
         } else {
             if (n_non_neg > n_min) {
                 double g = dt * f_inc;
-                dt = g < dt_max ? g : dt_max;
+                dt = dt_max < g ? dt_max : g; /* std::min(g, dt_max) */
                 alpha *= f_a;
             }
             n_non_neg++;

@@ -1,0 +1,183 @@
+"""GPU parity: the sm_103a kernels, called through the C ABI, against the
+reference's own results (tests/golden) and the oracle.
+
+Tolerances
+  FP64 plain kernel   same operation order as the reference, compiled without
+                      FMA contraction: bit-identical for LJ/Coulomb terms; with
+                      Morse (exp) or the cuFFT external field, last-bit
+                      differences may change a FIRE decision on a few points,
+                      so those cases require 99% identical step counts and the
+                      tip within 1e-6 A everywhere else.
+  FP32C kernel        the metric's bar: tip within 1e-3 A and Fz within 1e-3
+                      relative (denominator max(|Fz_ref|, 0.01 = ftol)) on at
+                      least 99.5% of points; no point beyond 0.05 A.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from conftest import ERROR_CASES, POINT_CASES, golden
+from mechafm_gb300 import _abi
+from mechafm_gb300.scan import Input, Scan, run_batch
+
+pytestmark = pytest.mark.gpu
+
+EXACT_CASES = {"graphene_ef", "graphene_euler", "graphene_sd", "graphene_pbc", "graphene_grid",
+               "graphene_ovwrt"}
+TIP_TOL = 1e-3
+FZ_TOL = 1e-3
+FZ_FLOOR = 0.01
+
+
+def run_case(case, precision, **kw):
+    desc = Input(case.input).desc()
+    scan = Scan(desc, device=0)
+    parts = []
+    for c0, c1 in case.columns(desc.c.ny):
+        p, _ = scan.run(precision, col_begin=c0, col_end=c1, **kw)
+        parts.append(p)
+    scan.close()
+    return np.concatenate(parts)
+
+
+def fz_rel(pts, ref_force):
+    return np.abs(pts["force"][:, 2] - ref_force[:, 2]) / np.maximum(np.abs(ref_force[:, 2]), FZ_FLOOR)
+
+
+@pytest.mark.parametrize("name", POINT_CASES)
+def test_fp64_matches_reference(name):
+    case = golden(name)
+    ref = case.ref
+    pts = run_case(case, _abi.FP64)
+    if name in EXACT_CASES:
+        np.testing.assert_array_equal(pts["steps"], ref["steps"])
+        np.testing.assert_array_equal(pts["tip"], ref["tip"])
+        np.testing.assert_array_equal(pts["force"], ref["force"])
+        np.testing.assert_array_equal(pts["energy"], ref["energy"])
+    else:
+        same = pts["steps"] == ref["steps"]
+        assert same.mean() >= 0.99, same.mean()
+        d = np.abs(pts["tip"] - ref["tip"]).max(axis=1)
+        assert d[same].max() < 1e-6, d[same].max()
+        assert d.max() < 0.05
+
+
+@pytest.mark.parametrize("name", POINT_CASES)
+def test_fp32c_within_tolerance_of_reference(name):
+    case = golden(name)
+    ref = case.ref
+    pts = run_case(case, _abi.FP32C)
+    tip_err = np.abs(pts["tip"] - ref["tip"]).max(axis=1)
+    fz = fz_rel(pts, ref["force"])
+    ok = (tip_err <= TIP_TOL) & (fz <= FZ_TOL)
+    assert ok.mean() >= 0.995, (ok.mean(), tip_err.max(), fz.max())
+    assert tip_err.max() < 0.05, tip_err.max()
+    # the maxsteps flag matches wherever the step counts match
+    both = pts["steps"] == ref["steps"]
+    assert both.mean() > 0.8
+
+
+@pytest.mark.parametrize("name", [n for n in POINT_CASES if golden(n).meta["sample"]])
+@pytest.mark.parametrize("precision", [_abi.FP64, _abi.FP32C])
+def test_samples_match_reference(name, precision):
+    case = golden(name)
+    desc = Input(case.input).desc()
+    scan = Scan(desc, device=0)
+    what = int(case.ref["sample_mode"])
+    fe = scan.sample(case.ref["sample_pts"], precision=precision, what=what)
+    ref = case.ref["sample_fe"]
+    scale = np.maximum(np.abs(ref), 1e-2)
+    tol = (1e-9 if name != "graphene_grid" else 0.0) if precision == _abi.FP64 else 2e-5
+    assert (np.abs(fe - ref) / scale).max() <= tol
+
+
+@pytest.mark.parametrize("name", ERROR_CASES)
+def test_reference_error_reproduced(name):
+    case = golden(name)
+    desc = Input(case.input).desc()
+    with pytest.raises(_abi.MafmError) as e:
+        Scan(desc, device=0)
+    assert e.value.code == _abi.MAFM_E_RANGE
+    assert case.meta["error"].split("Value:")[0].strip() in e.value.msg
+
+
+def test_fp64_matches_oracle_on_random_columns():
+    """C2-sized scan: random columns, FP64 GPU against the oracle port."""
+    case = golden("cluster_ef")
+    desc = Input(case.input).desc()
+    scan = Scan(desc, device=0)
+    rng = np.random.default_rng(11)
+    for c0 in rng.integers(0, desc.n_columns - 8, size=4):
+        got, st = scan.run(_abi.FP64, col_begin=int(c0), col_end=int(c0) + 8)
+        want, steps = oracle.run(desc, int(c0), int(c0) + 8)
+        assert int(st.total_steps) == steps
+        same = got["steps"] == want["steps"]
+        assert same.mean() >= 0.99
+        assert np.abs(got["tip"] - want["tip"]).max(axis=1)[same].max() < 1e-6
+
+
+def test_lane_counts_agree():
+    """Every lanes-per-column variant of the FP32 kernel meets the bar against FP64."""
+    case = golden("cluster_ef")
+    ref = case.ref
+    base = None
+    for lanes in (1, 2, 4, 8, 16, 32):
+        pts = run_case(case, _abi.FP32C, lanes=lanes)
+        tip_err = np.abs(pts["tip"] - ref["tip"]).max(axis=1)
+        ok = (tip_err <= TIP_TOL) & (fz_rel(pts, ref["force"]) <= FZ_TOL)
+        assert ok.mean() >= 0.995, (lanes, ok.mean())
+        if lanes == 1:
+            base = pts
+    again = run_case(case, _abi.FP32C, lanes=1)
+    np.testing.assert_array_equal(again["tip"], base["tip"])   # deterministic
+
+
+def test_batch_equals_single_runs():
+    """A multi-scan persistent launch gives the same bits as one launch per scan."""
+    names = ["graphene_euler", "cluster_rk4", "cluster_f", "graphene_grid"]
+    scans, singles = [], []
+    for n in names:
+        desc = Input(golden(n).input).desc()
+        s = Scan(desc, device=0)
+        scans.append(s)
+        singles.append(s.run(_abi.FP32C, lanes=1)[0])
+    outs, stats = run_batch(scans, lanes=1)
+    for a, b in zip(outs, singles):
+        np.testing.assert_array_equal(a["tip"], b["tip"])
+        np.testing.assert_array_equal(a["steps"], b["steps"])
+    assert stats.total_steps == sum(int(s["steps"].sum()) for s in singles)
+
+
+def test_column_ranges_compose():
+    case = golden("graphene_pbc")
+    desc = Input(case.input).desc()
+    scan = Scan(desc, device=0)
+    full, _ = scan.run(_abi.FP64, col_begin=0, col_end=600)
+    a, _ = scan.run(_abi.FP64, col_begin=0, col_end=250)
+    b, _ = scan.run(_abi.FP64, col_begin=250, col_end=600)
+    np.testing.assert_array_equal(full["tip"], np.concatenate([a, b])["tip"])
+
+
+def test_rigid_grid_exit_is_an_error():
+    """The tip leaving a rigid grid stops the reference (force_grid.cpp:236-240)."""
+    import tempfile
+    from mechafm_gb300 import synth
+    with tempfile.TemporaryDirectory() as tmp:
+        inp = synth.graphene_72(area=6.0, step=0.5, zlow=6.0, rigidgrid="on").write(tmp)
+        scan = Scan(Input(inp).desc(), device=0)
+        with pytest.raises(_abi.MafmError) as e:
+            scan.run(_abi.FP64)
+        assert e.value.code == _abi.MAFM_E_RANGE
+
+
+def test_no_atoms_and_single_point():
+    case = golden("graphene_ef")
+    desc = Input(case.input).desc()
+    desc.c.n_atoms = 0
+    desc.c.nx = desc.c.ny = desc.c.nz = 1
+    scan = Scan(desc, device=0)
+    got, _ = scan.run(_abi.FP64)
+    want, _ = oracle.run(desc)
+    np.testing.assert_array_equal(got["tip"], want["tip"])
+    got32, _ = scan.run(_abi.FP32C)
+    assert np.abs(got32["tip"] - want["tip"]).max() < 1e-6
