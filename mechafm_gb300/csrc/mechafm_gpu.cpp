@@ -1,0 +1,132 @@
+// mechafm_gpu.cpp — `mechafm-gpu INPUT-FILE [OUTPUT-FOLDER]`, a drop-in for the
+// reference's `mechafm-omp` (src/mechafm.cpp:209-233) on one GPU.
+//
+// Same arguments, input/xyz/parameter/cube files, stdout banners and option
+// echo, error messages and exit status, scan-%06.3f.dat[.gz] files and
+// statistics.txt.  The relaxation runs through libmafm's C ABI.  By default it
+// runs the FP64 kernel, whose results are those of the reference; setting
+// MAFM_PRECISION=fp32c selects the FP32-compensated kernel.  MAFM_DEVICE picks
+// the GPU (default 0).
+#include <chrono>
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "mafm.h"
+
+namespace {
+
+void pretty(const char* fmt, ...) {
+    char buf[2048];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    fprintf(stdout, "+- %s\n", buf);
+}
+
+[[noreturn]] void error(const char* msg) {
+    // messages.cpp:12-27 of the reference
+    fprintf(stderr, "+- ERROR (on process %d): %s\n", 0, msg);
+    exit(1);
+}
+
+void check(int code) {
+    if (code != MAFM_OK) error(mafm_last_error());
+}
+
+}  // namespace
+
+int main(int argc, char* argv[]) {
+    // parseCommandLine (parse.cpp:30-80)
+    fprintf(stdout, "+ - - - - - - - - - - - - - - - - - - - - - - - - - - - - - - +\n");
+    fprintf(stdout, "|                   Mechanical AFM Model                      |\n");
+    fprintf(stdout, "|  Based on: P. Hapala et al, Phys. Rev. B, 90:085421 (2014)  |\n");
+    fprintf(stdout, "|                  This implementation by                     |\n");
+    fprintf(stdout, "|             Peter Spijker and Olli Keisanen                 |\n");
+    fprintf(stdout, "|          2014-2015 (c) Aalto University, Finland            |\n");
+    fprintf(stdout, "+ - - - - - - - - - - - - - - - - - - - - - - - - - - - - - - +\n");
+    if (argc < 2) error("Specify an input file to be read!");
+    if (argc > 3) error("Too many command line arguments!");
+    std::string outdir;
+    if (argc == 3) {
+        outdir = argv[2];
+        if (outdir.empty() || outdir.back() != '/') outdir += '/';
+        std::string cmd = "mkdir -p " + outdir;
+        if (system(cmd.c_str()) != 0) error(("cannot create " + outdir).c_str());
+    }
+    const char* prec_env = getenv("MAFM_PRECISION");
+    const int precision = (prec_env && !strcmp(prec_env, "fp32c")) ? MAFM_FP32C : MAFM_FP64;
+    const char* dev_env = getenv("MAFM_DEVICE");
+    const int device = dev_env ? atoi(dev_env) : 0;
+
+    mafm_input* in = nullptr;
+    check(mafm_input_load(argv[1], 1, &in));
+    mafm_scan_desc d;
+    check(mafm_input_desc(in, &d));
+    int32_t gzip = 0, statistics = 0, bufsize = 0;
+    check(mafm_input_output_opts(in, &gzip, &statistics, &bufsize));
+
+    // openUniverse (mechafm.cpp:37-80)
+    const int n_total = d.nx * d.ny * d.nz;
+    pretty("3D data grid is: %d x %d x %d (%d in total)", d.nx, d.ny, d.nz, n_total);
+    const auto t_start = std::chrono::system_clock::now();
+
+    // Simulation::initialize / buildInteractions messages (simulation.cpp:324,416,443,500)
+    if (d.use_external_potential)
+        pretty("Calculating energy and force on grid from external electrostatic potential.");
+    mafm_scan* scan = nullptr;
+    check(mafm_scan_create(device, &d, &scan));
+    if (d.use_external_potential) pretty("Done!");
+    if (d.rigidgrid) {
+        int32_t n[3];
+        double basis[9], origin[3];
+        check(mafm_scan_grid_info(scan, 0, n, basis, origin));
+        pretty("Computing 3D force grid: %d, %d, %d (%d grid points)", n[0], n[1], n[2],
+               n[0] * n[1] * n[2]);
+        pretty("Done!");
+    }
+
+    // Simulation::run (simulation.cpp:67-143): the x rows in ten chunks, with
+    // the reference's progress lines.
+    pretty("Starting simulation");
+    std::vector<mafm_point> pts((size_t)n_total);
+    uint64_t total_steps = 0;
+    const int chunks = 10;
+    for (int c = 0; c < chunks; ++c) {
+        const int i0 = (int)((long long)d.nx * c / chunks), i1 = (int)((long long)d.nx * (c + 1) / chunks);
+        if (i1 <= i0) continue;
+        mafm_run_opts o{};
+        o.precision = precision;
+        o.col_begin = i0 * d.ny;
+        o.col_end = i1 * d.ny;
+        mafm_run_stats st{};
+        check(mafm_run(scan, &o, pts.data() + (size_t)o.col_begin * d.nz, &st, nullptr));
+        total_steps += st.total_steps;
+        pretty("Finished %4.1f %% of the simulation", 100.0 * i1 / d.nx);
+    }
+    check(mafm_write_output(in, pts.data(), outdir.c_str(), gzip));
+    check(mafm_scan_destroy(scan));
+
+    // finalize (mechafm.cpp:103-154)
+    const auto t_end = std::chrono::system_clock::now();
+    const double secs = std::chrono::duration<double>(t_end - t_start).count();
+    pretty("Simulation run finished");
+    pretty("Statistics:");
+    pretty("    Computed %d tip positions", n_total);
+    pretty("    Needed %ld minimization steps in total", (long)total_steps);
+    pretty("    Which means approximately %.2f minimization steps per tip position",
+           (double)total_steps / n_total);
+    pretty("    The simulation wall time is %.2f seconds", secs);
+    pretty("    The entire simulation took %.2f seconds", secs);
+    pretty("");
+    if (statistics) check(mafm_write_statistics(in, outdir.c_str(), total_steps, secs, secs));
+    // closeParallelUniverse (mechafm.cpp:183-207)
+    pretty("How many x,y points did each process handle:");
+    pretty("    Process %2d: %6d x,y points", 0, d.nx * d.ny);
+    mafm_input_free(in);
+    return 0;
+}

@@ -93,6 +93,41 @@ def sample_points(inp_name: str, spec, n: int = 64, seed: int = 5):
     return np.column_stack([x, y, z])
 
 
+def cli_cases():
+    """Tiny inputs run through the reference's own executable (oracle/_ref/mechafm-omp)."""
+    ca, cb, cc = graphene_cell()
+    return [
+        ("cli_cluster", synth.cluster_60(area=0.2, step=0.1, zhigh=10.0, zlow=9.8, dz=0.1)),
+        ("cli_pbc", synth.graphene_72(area=20.0, step=10.0, zhigh=10.0, zlow=9.8, dz=0.1,
+                                      vdw_pbc="on", cell_a=_vec(ca), cell_b=_vec(cb),
+                                      cell_c=_vec(cc))),
+    ]
+
+
+def make_cli_fixture(name, spec):
+    """Sorted rows of every scan-*.dat file, and statistics.txt without its timing lines."""
+    folder = os.path.join(HERE, name)
+    if os.path.isdir(folder):
+        shutil.rmtree(folder)
+    inp = spec.write(folder)
+    out = os.path.join(folder, "_out")
+    subprocess.run([oracle.REF_CLI, os.path.abspath(inp), out], check=True, cwd=folder,
+                   stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+    rows = []
+    for fn in sorted(os.listdir(out)):
+        if fn.startswith("scan-"):
+            with open(os.path.join(out, fn)) as f:
+                rows += [fn + "\t" + l.rstrip("\n") for l in f]
+    with open(os.path.join(folder, "cli_rows.txt"), "w") as f:
+        f.write("\n".join(sorted(rows)) + "\n")
+    with open(os.path.join(out, "statistics.txt")) as f:
+        stats = f.readlines()[:4]
+    with open(os.path.join(folder, "cli_statistics_head.txt"), "w") as f:
+        f.writelines(stats)
+    shutil.rmtree(out)
+    return {"input": os.path.basename(inp), "cli": True, "rows": len(rows)}
+
+
 def main():
     oracle.build()
     if not oracle.ref_available():
@@ -121,6 +156,16 @@ def main():
             "tip": rec[:, 4:7], "force": rec[:, 13:16], "energy": rec[:, 16],
             "r": rec[:, 20], "angle": rec[:, 21], "block": np.array(block, dtype=np.int32),
         }
+        sysinfo = oracle.ref_system(inp, os.path.join(folder, "_sys.txt"))
+        os.remove(os.path.join(folder, "_sys.txt"))
+        atoms = sysinfo["atoms"]
+        out["sys_types"] = np.array([a[0] for a in atoms])
+        out["sys_pos"] = np.array([a[1:4] for a in atoms])
+        out["sys_charge"] = np.array([a[4] for a in atoms])
+        out["sys_tip_dummy_d"] = np.array(sysinfo["tip_dummy_d"])
+        out["sys_offset"] = np.array(sysinfo["offset"])
+        out["sys_n_points"] = np.array(sysinfo["n_points"], dtype=np.int32)
+        out["sys_xyz_charges"] = np.array(int(sysinfo["xyz_charges"]), dtype=np.int32)
         if sample:
             pts = sample_points(name, spec)
             fe = oracle.ref_sample(inp, pts, sample, os.path.join(folder, "_s"))
@@ -133,6 +178,9 @@ def main():
         manifest[name] = {"input": os.path.basename(inp), "block": list(block),
                           "points": int(len(rec)), "sample": sample}
         print(name, len(rec), "points, mean steps", rec[:, 3].mean())
+    for name, spec in cli_cases():
+        manifest[name] = make_cli_fixture(name, spec)
+        print(name, manifest[name]["rows"], "rows from the reference executable")
     with open(os.path.join(HERE, "manifest.json"), "w") as f:
         json.dump(manifest, f, indent=1, sort_keys=True)
 

@@ -1,0 +1,45 @@
+"""Output parity with the reference executable: scan-%06.3f.dat rows and
+statistics.txt written by libmafm (mafm_write_output / mafm_write_statistics)
+from oracle points are byte-identical to what `mechafm-omp` wrote (rows are
+compared sorted: the reference writes them in thread order,
+simulation.cpp:176)."""
+import ctypes as C
+import gzip
+import os
+
+import pytest
+
+import oracle
+from conftest import GOLDEN, MANIFEST
+from mechafm_gb300 import _abi
+from mechafm_gb300.scan import Input
+
+CLI_CASES = sorted(k for k, v in MANIFEST.items() if v.get("cli"))
+
+
+def rows_of(folder):
+    rows = []
+    for fn in sorted(os.listdir(folder)):
+        if fn.startswith("scan-"):
+            path = os.path.join(folder, fn)
+            opener = gzip.open if fn.endswith(".gz") else open
+            with opener(path, "rt") as f:
+                name = fn[:-3] if fn.endswith(".gz") else fn
+                rows += [name + "\t" + l.rstrip("\n") for l in f]
+    return sorted(rows)
+
+
+@pytest.mark.parametrize("name", CLI_CASES)
+@pytest.mark.parametrize("use_gzip", [False, True])
+def test_scan_files_match_reference_executable(name, use_gzip, tmp_path):
+    folder = os.path.join(GOLDEN, name)
+    inp = Input(os.path.join(folder, MANIFEST[name]["input"]))
+    desc = inp.desc()
+    pts, steps = oracle.run(desc)
+    inp.write_output(pts, str(tmp_path), gzip=use_gzip)
+    want = open(os.path.join(folder, "cli_rows.txt")).read().splitlines()
+    assert rows_of(str(tmp_path)) == want
+    out = str(tmp_path) + "/"
+    _abi.check(_abi.lib().mafm_write_statistics(inp.handle, out.encode(), steps, 1.0, 1.0))
+    head = open(os.path.join(tmp_path, "statistics.txt")).readlines()[:4]
+    assert head == open(os.path.join(folder, "cli_statistics_head.txt")).readlines()
