@@ -50,6 +50,8 @@ def parse():
     ap.add_argument("--cpu-columns", type=int, default=0,
                     help="columns of the bounded CPU sample (0 = sized to ~15 s)")
     ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--pixels", type=int, default=401,
+                    help="pixels per side (401 = the benchmark workload; smaller for profiling)")
     return ap.parse_args()
 
 
@@ -60,10 +62,10 @@ def dist_env():
     return rank, world, local
 
 
-def make_workload(tmp):
+def make_workload(tmp, pixels=401):
     from mechafm_gb300 import synth
     from mechafm_gb300.scan import Input
-    inp = synth.cluster_60().write(tmp)
+    inp = synth.cluster_60(area=0.05 * (pixels - 1)).write(tmp)
     I = Input(inp)
     return I, I.desc()
 
@@ -186,7 +188,7 @@ def ours(args, rank, world, local):
         import torch.distributed as dist
         dist.init_process_group("nccl")
     tmp = tempfile.mkdtemp()
-    I, desc = make_workload(tmp)
+    I, desc = make_workload(tmp, args.pixels)
     n_pts = desc.n_points
     scan = Scan(desc, device=dev)
     out = torch.empty(n_pts * 64, dtype=torch.uint8, device=f"cuda:{dev}")
@@ -248,7 +250,9 @@ def ours(args, rank, world, local):
         # FP64 plain kernel on a column subset: speed and the FP32C error against it.
         fp64 = None
         if not args.no_fp64:
-            cols = 4096
+            # enough columns for two FP64 blocks of 128 threads on every SM
+            props = torch.cuda.get_device_properties(dev)
+            cols = min(desc.n_columns, props.multi_processor_count * 256)
             c0 = desc.n_columns // 2 - cols // 2
             p64, s64 = scan.run(_abi.FP64, col_begin=c0, col_end=c0 + cols)
             p32, s32 = scan.run(_abi.FP32C, col_begin=c0, col_end=c0 + cols)

@@ -87,7 +87,9 @@ def test_samples_match_reference(name, precision):
     fe = scan.sample(case.ref["sample_pts"], precision=precision, what=what)
     ref = case.ref["sample_fe"]
     scale = np.maximum(np.abs(ref), 1e-2)
-    tol = (1e-9 if name != "graphene_grid" else 0.0) if precision == _abi.FP64 else 2e-5
+    # FP32 lookups: fractional cell coordinates carry ~1e-6 of a cell, which on
+    # the steep 0.25 A external-field cells is a few 1e-5 relative.
+    tol = (1e-9 if name != "graphene_grid" else 0.0) if precision == _abi.FP64 else 1e-4
     assert (np.abs(fe - ref) / scale).max() <= tol
 
 
