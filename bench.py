@@ -50,6 +50,7 @@ def parse():
     ap.add_argument("--cpu-columns", type=int, default=0,
                     help="columns of the bounded CPU sample (0 = sized to ~15 s)")
     ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--lanes", type=int, default=0, help="lanes per column (0 = default)")
     ap.add_argument("--pixels", type=int, default=401,
                     help="pixels per side (401 = the benchmark workload; smaller for profiling)")
     return ap.parse_args()
@@ -197,12 +198,14 @@ def ours(args, rank, world, local):
     sptr = stream.cuda_stream
 
     def one_step():
-        return scan.run_device(out.data_ptr(), precision=_abi.FP32C, stream=sptr)
+        return scan.run_device(out.data_ptr(), precision=_abi.FP32C, stream=sptr,
+                               lanes=args.lanes)
 
     for _ in range(args.warmup):
         one_step()
     torch.cuda.synchronize()
-    st = scan.run_device(out.data_ptr(), precision=_abi.FP32C, stream=sptr, stats=True)
+    st = scan.run_device(out.data_ptr(), precision=_abi.FP32C, stream=sptr, stats=True,
+                         lanes=args.lanes)
     steps_per_scan = int(st.total_steps)
     evals_per_scan = int(st.force_evals)
     pairs_per_scan = int(st.pair_evals)
