@@ -208,6 +208,29 @@ int mafm_run(mafm_scan* scan, const mafm_run_opts* opts, mafm_point* out,
 int mafm_run_batch(mafm_scan* const* scans, int32_t n_scans, const mafm_run_opts* opts,
                    mafm_point* const* outs, mafm_run_stats* stats, void* stream);
 
+/* mafm_run_batch without any memory allocation.  No counterpart in the
+ * reference: it exists for callers that cannot let a library call cudaMalloc
+ * or cudaFree (their own capped memory pool, no implicit device-wide
+ * synchronisation from cudaFree in a steady state, exact accounting of device
+ * memory on a shared GPU).  The relax kernel's scratch — work-queue counters
+ * and per-scan descriptors — lives in a fixed device array of the library
+ * (256 B + MAFM_NOALLOC_MAX_SCANS descriptors of under 1 KB each), held by
+ * every GPU that loads the library until the process exits.
+ *   - At most MAFM_NOALLOC_MAX_SCANS scans per call, else MAFM_E_RANGE.
+ *   - MAFM_FP32C, whole scans; every outs[s] must be device memory.
+ *   - A scan with a rigid grid must have its FP32 grid built already (one
+ *     mafm_run with MAFM_FP32C does that), else MAFM_E_INVALID.
+ *   - The first call on a device looks up the array's device address; make
+ *     that first call before any stream capture.
+ *   - All calls share the array and it keeps the last call's contents; each
+ *     call clears its counters first.  Calls that overlap on the GPU race:
+ *     order them on one stream or with events.
+ *   - stats may be NULL; when given, the call synchronises the stream
+ *     (kernel_ms is left 0). */
+#define MAFM_NOALLOC_MAX_SCANS 32
+int mafm_run_batch_noalloc(mafm_scan* const* scans, int32_t n_scans, const mafm_run_opts* opts,
+                           mafm_point* const* outs, mafm_run_stats* stats, void* stream);
+
 /* Evaluate the tip–surface force and energy at n given tip positions
  * (System::evalTipSurfaceForces, system.cpp:41-51): pairs, external field or
  * rigid grid, whatever the scan uses.  what: 0 = all tip–surface terms,

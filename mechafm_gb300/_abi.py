@@ -24,6 +24,7 @@ TERM_E, TERM_F, TERM_EF = 0, 1, 2
 PAIR_LJ, PAIR_MORSE = 0, 1
 FP64, FP32C = 0, 1
 PT_MAXSTEPS, PT_NONFINITE, PT_OUTSIDE = 1, 2, 4
+NOALLOC_MAX_SCANS = 32
 
 
 class Pair(C.Structure):
@@ -92,6 +93,8 @@ SIGNATURES = {
     "mafm_run": (C.c_int, [_P, C.POINTER(RunOpts), _P, C.POINTER(RunStats), _P]),
     "mafm_run_batch": (C.c_int, [C.POINTER(_P), C.c_int32, C.POINTER(RunOpts),
                                  C.POINTER(_P), C.POINTER(RunStats), _P]),
+    "mafm_run_batch_noalloc": (C.c_int, [C.POINTER(_P), C.c_int32, C.POINTER(RunOpts),
+                                         C.POINTER(_P), C.POINTER(RunStats), _P]),
     "mafm_scan_sample": (C.c_int, [_P, C.c_int32, C.c_int32, _P, C.c_int64, _P]),
     "mafm_scan_grid_info": (C.c_int, [_P, C.c_int32, C.c_int32 * 3, C.c_double * 9,
                                       C.c_double * 3]),

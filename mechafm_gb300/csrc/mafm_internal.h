@@ -165,3 +165,14 @@ cudaError_t launch_grid_build32(const ScanParams& p, const GridView& g, float4* 
 int sm_count();
 
 }  // namespace mafm
+
+// Read-only views of a scan for entry points defined outside scan.cu.
+namespace mafm {
+int scan_device(const mafm_scan* s);
+long long scan_columns(const mafm_scan* s);
+int scan_direct_terms(const mafm_scan* s);
+bool scan_fp32_ready(const mafm_scan* s);   // FP32 tables on the device (rigid grid built if used)
+BatchScan scan_batch_entry(const mafm_scan* s, mafm_point* out);
+Relax32Config relax32_config(long long n_cols, int max_terms, const mafm_run_opts* o);
+void check_run_errors(const RunCounters& c);
+}  // namespace mafm

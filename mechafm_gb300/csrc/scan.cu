@@ -808,3 +808,33 @@ int mafm_scan_grid_copy(const mafm_scan* scan, int32_t what, double* out) {
 }
 
 }  // extern "C"
+
+namespace mafm {
+
+int scan_device(const mafm_scan* s) { return s->device; }
+
+long long scan_columns(const mafm_scan* s) { return (long long)s->d.nx * s->d.ny; }
+
+int scan_direct_terms(const mafm_scan* s) { return s->d.rigidgrid ? 0 : s->P.n_terms; }
+
+bool scan_fp32_ready(const mafm_scan* s) { return !s->d.rigidgrid || s->grid32_built; }
+
+BatchScan scan_batch_entry(const mafm_scan* s, mafm_point* out) {
+    BatchScan b{};
+    b.p = build_params(*s);
+    b.out = out;
+    b.tile_begin = 0;
+    b.col_begin = 0;
+    b.col_end = s->d.nx * s->d.ny;
+    b.n_pairs_per_eval = s->n_pairs_per_eval;
+    b.has_coulomb = s->has_coulomb;
+    return b;
+}
+
+Relax32Config relax32_config(long long n_cols, int max_terms, const mafm_run_opts* o) {
+    return default_config(n_cols, max_terms, o);
+}
+
+void check_run_errors(const RunCounters& c) { check_device_errors(c); }
+
+}  // namespace mafm
