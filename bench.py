@@ -51,6 +51,8 @@ def parse():
                     help="columns of the bounded CPU sample (0 = sized to ~15 s)")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--lanes", type=int, default=0, help="lanes per column (0 = default)")
+    ap.add_argument("--sweep", action="store_true",
+                    help="also time every lanes-per-column value and print one line each")
     ap.add_argument("--pixels", type=int, default=401,
                     help="pixels per side (401 = the benchmark workload; smaller for profiling)")
     return ap.parse_args()
@@ -247,6 +249,21 @@ def ours(args, rank, world, local):
         if i > 0:
             e2e_times.append(t1 - t0)
     e2e_value = world * n_pts / float(np.mean(e2e_times))
+
+    if args.sweep and rank == 0:
+        for lanes in (1, 2, 4, 8, 16, 32):
+            best = 1e30
+            for _ in range(2):
+                flush.zero_()
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                scan.run_device(out.data_ptr(), precision=_abi.FP32C, stream=sptr, lanes=lanes)
+                e1.record(stream)
+                torch.cuda.synchronize()
+                best = min(best, e0.elapsed_time(e1))
+            print(json.dumps({"sweep_lanes": lanes, "ms": best, "points_per_s": n_pts / best * 1e3}),
+                  file=sys.stderr)
 
     line = None
     if rank == 0:

@@ -31,7 +31,7 @@ namespace mafm {
 namespace {
 
 constexpr unsigned kFull = 0xffffffffu;
-constexpr int kChunk = 4;                 // terms summed plainly before a compensated add
+constexpr int kChunk = 8;                 // terms summed plainly before a compensated add
 constexpr long long kWaitLimit = 1ll << 24;  // bounded mbarrier wait (iterations)
 
 enum : int { PH_EVAL0 = 0, PH_EVAL1 = 1, PH_EVAL2 = 2, PH_EVAL3 = 3, PH_OUT = 4 };
@@ -84,15 +84,18 @@ struct Acc {
 #pragma unroll
         for (int m = 0; m < 4; ++m) s[m] = c[m] = 0.f;
     }
+    // Kahan step: c carries the negated low part lost so far.
     __device__ __forceinline__ void add(const float v[4]) {
 #pragma unroll
         for (int m = 0; m < 4; ++m) {
-            float t, e;
-            two_sum(s[m], v[m], t, e);
+            const float y = v[m] - c[m];
+            const float t = s[m] + y;
+            c[m] = (t - s[m]) - y;
             s[m] = t;
-            c[m] += e;
         }
     }
+    // value = s - c
+    __device__ __forceinline__ float val(int m) const { return s[m] - c[m]; }
     // Combine across the G lanes of a group; every lane ends with the same sums
     // (two-sum and + are commutative, so partners compute identical values).
     template <int G>
@@ -106,7 +109,7 @@ struct Acc {
                 float t, e;
                 two_sum(s[m], so, t, e);
                 s[m] = t;
-                c[m] = (c[m] + co) + e;
+                c[m] = (c[m] + co) - e;
             }
         }
     }
@@ -145,29 +148,66 @@ __device__ __forceinline__ void pair32(const AtomRec32& t, float dx, float dy, f
     v[3] += e;
 }
 
-// Trilinear lookup on an FP32 grid (ForceGrid::interpolate).  q = position -
-// grid origin.  Sets *outside when clamped, ERR_GRID_INDEX when a corner of a
-// non-periodic grid falls outside (then clamped, never read out of bounds).
-__device__ void interp32(const GridView& g, float qx, float qy, float qz, float v[4],
-                         int& outside, unsigned& err) {
-    float pb[3];
+// FP32 view of a trilinear grid (ForceGrid, force_grid.hpp:15-51), converted
+// from the FP64 GridView once per scan: reciprocal steps (orthogonal) or the
+// inverse basis, and the origin split into hi + lo floats.
+struct Lookup32 {
+    const float4* g;
+    int n[3];
+    int periodic, orthogonal;
+    float inv[9];
+    float org_hi[3], org_lo[3];
+};
+
+__device__ Lookup32 make_lookup(const GridView& g) {
+    Lookup32 L;
+    L.g = g.g32;
+    for (int a = 0; a < 3; ++a) {
+        L.n[a] = g.n[a];
+        const DF o = df_split(g.origin[a]);
+        L.org_hi[a] = o.hi;
+        L.org_lo[a] = o.lo;
+    }
+    L.periodic = g.periodic;
+    L.orthogonal = g.orthogonal;
+    for (int k = 0; k < 9; ++k) L.inv[k] = 0.f;
     if (g.orthogonal) {
-        pb[0] = qx / (float)g.basis[0];
-        pb[1] = qy / (float)g.basis[4];
-        pb[2] = qz / (float)g.basis[8];
+        L.inv[0] = (float)(1.0 / g.basis[0]);
+        L.inv[4] = (float)(1.0 / g.basis[4]);
+        L.inv[8] = (float)(1.0 / g.basis[8]);
     } else {
-        pb[0] = (float)g.inv[0] * qx + (float)g.inv[1] * qy + (float)g.inv[2] * qz;
-        pb[1] = (float)g.inv[3] * qx + (float)g.inv[4] * qy + (float)g.inv[5] * qz;
-        pb[2] = (float)g.inv[6] * qx + (float)g.inv[7] * qy + (float)g.inv[8] * qz;
+        for (int k = 0; k < 9; ++k) L.inv[k] = (float)g.inv[k];
+    }
+    return L;
+}
+
+// Trilinear lookup (ForceGrid::interpolate) at a double-float position; adds
+// {Fx,Fy,Fz,E} into v.  Sets outside when clamped at the border, and
+// ERR_GRID_INDEX when a corner of a non-periodic grid falls outside (the
+// corner is then clamped, so no read leaves the grid).
+__device__ void interp32(const Lookup32& L, DF px, DF py, DF pz, float v[4], int& outside,
+                         unsigned& err) {
+    const float qx = (px.hi - L.org_hi[0]) + (px.lo - L.org_lo[0]);
+    const float qy = (py.hi - L.org_hi[1]) + (py.lo - L.org_lo[1]);
+    const float qz = (pz.hi - L.org_hi[2]) + (pz.lo - L.org_lo[2]);
+    float pb[3];
+    if (L.orthogonal) {
+        pb[0] = qx * L.inv[0];
+        pb[1] = qy * L.inv[4];
+        pb[2] = qz * L.inv[8];
+    } else {
+        pb[0] = L.inv[0] * qx + L.inv[1] * qy + L.inv[2] * qz;
+        pb[1] = L.inv[3] * qx + L.inv[4] * qy + L.inv[5] * qz;
+        pb[2] = L.inv[6] * qx + L.inv[7] * qy + L.inv[8] * qz;
     }
     int gp[3];
     float d[3];
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
         gp[a] = (int)floorf(pb[a]);
-        if (!g.periodic) {
+        if (!L.periodic) {
             if (gp[a] < 0) { gp[a] = 0; outside = 1; }
-            else if (gp[a] >= g.n[a]) { gp[a] = g.n[a] - 1; outside = 1; }
+            else if (gp[a] >= L.n[a]) { gp[a] = L.n[a] - 1; outside = 1; }
         }
         d[a] = pb[a] - (float)gp[a];
     }
@@ -175,25 +215,24 @@ __device__ void interp32(const GridView& g, float qx, float qy, float qz, float 
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
         int x0 = gp[a], x1 = gp[a] + 1;
-        if (g.periodic) {
-            x0 %= g.n[a]; if (x0 < 0) x0 += g.n[a];
-            x1 %= g.n[a]; if (x1 < 0) x1 += g.n[a];
-        } else if (x1 >= g.n[a]) {
+        if (L.periodic) {
+            x0 %= L.n[a]; if (x0 < 0) x0 += L.n[a];
+            x1 %= L.n[a]; if (x1 < 0) x1 += L.n[a];
+        } else if (x1 >= L.n[a]) {
             err |= ERR_GRID_INDEX;
-            x1 = g.n[a] - 1;
+            x1 = L.n[a] - 1;
         }
         lo[a] = x0;
         hi[a] = x1;
     }
-    const long long n12 = (long long)g.n[1] * g.n[2];
-    const float4* G4 = g.g32;
+    const long long n12 = (long long)L.n[1] * L.n[2];
     float4 s[8];
 #pragma unroll
     for (int c = 0; c < 8; ++c) {
         const int x = (c >> 2) ? hi[0] : lo[0];
         const int y = ((c >> 1) & 1) ? hi[1] : lo[1];
         const int z = (c & 1) ? hi[2] : lo[2];
-        s[c] = __ldg(G4 + (long long)x * n12 + (long long)y * g.n[2] + z);
+        s[c] = __ldg(L.g + (long long)x * n12 + (long long)y * L.n[2] + z);
     }
     const float dx = d[0], dy = d[1], dz = d[2];
     auto lerp3 = [&](float a0, float a1, float a2, float a3, float a4, float a5, float a6, float a7) {
@@ -206,15 +245,6 @@ __device__ void interp32(const GridView& g, float qx, float qy, float qz, float 
     v[1] += lerp3(s[0].y, s[1].y, s[2].y, s[3].y, s[4].y, s[5].y, s[6].y, s[7].y);
     v[2] += lerp3(s[0].z, s[1].z, s[2].z, s[3].z, s[4].z, s[5].z, s[6].z, s[7].z);
     v[3] += lerp3(s[0].w, s[1].w, s[2].w, s[3].w, s[4].w, s[5].w, s[6].w, s[7].w);
-}
-
-// Position minus a grid origin, from a double-float position.
-__device__ __forceinline__ void rel_origin(const GridView& g, DF px, DF py, DF pz, float& qx,
-                                           float& qy, float& qz) {
-    const DF ox = df_split(g.origin[0]), oy = df_split(g.origin[1]), oz = df_split(g.origin[2]);
-    qx = (px.hi - ox.hi) + (px.lo - ox.lo);
-    qy = (py.hi - oy.hi) + (py.lo - oy.lo);
-    qz = (pz.hi - oz.hi) + (pz.lo - oz.lo);
 }
 
 // System::setDummyXY (system.cpp:139-162) in FP64.
@@ -237,29 +267,71 @@ __device__ __forceinline__ void dummy_xy(const ScanParams& p, bool wrap, double 
     }
 }
 
-// vdW term of the dummy–tip pair in FP32; r = dummy - tip.
-__device__ __forceinline__ void td_vdw32(const ScanParams& p, float rx, float ry, float rz,
+// The scan's scalars in FP32, converted once per scan switch: the relax
+// loop then runs without FP64 instructions (the FP64 pipe of GB300 is 1/64
+// of the FP32 rate).
+struct WarpParams {
+    Lookup32 grid, es;
+    float dt0, dt_max, etol, ftol;
+    float td_p0, td_p1, td_p2, td_qq;
+    float harm_k, harm_r0;
+    DF dz;
+    int maxsteps, minimiser, integrator, minterm;
+    int ts_mode, td_kind, td_coul, nz;
+    int ny, col_begin, pad0, pad1;
+};
+
+__device__ void make_warp_params(const BatchScan& B, WarpParams& w) {
+    const ScanParams& P = B.p;
+    w.grid = make_lookup(P.grid);
+    w.es = make_lookup(P.es);
+    w.dt0 = (float)P.dt;
+    w.dt_max = (float)(10 * P.dt);
+    w.etol = (float)P.etol;
+    w.ftol = (float)P.ftol;
+    w.td_p0 = (float)P.td_p[0];
+    w.td_p1 = (float)P.td_p[1];
+    w.td_p2 = (float)P.td_p[2];
+    w.td_qq = (float)P.td_qq;
+    w.harm_k = (float)P.harm_k;
+    w.harm_r0 = (float)P.harm_r0;
+    w.dz = df_split(P.dz);
+    w.maxsteps = P.maxsteps;
+    w.minimiser = P.minimiser;
+    w.integrator = P.integrator;
+    w.minterm = P.minterm;
+    w.ts_mode = P.ts_mode;
+    w.td_kind = P.td_kind;
+    w.td_coul = P.td_coul;
+    w.nz = P.nz;
+    w.ny = P.ny;
+    w.col_begin = B.col_begin;
+    w.pad0 = w.pad1 = 0;
+}
+
+// vdW (+ Coulomb) term of the dummy–tip pair in FP32; r = dummy - tip.
+__device__ __forceinline__ void td_vdw32(const WarpParams& w, float rx, float ry, float rz,
                                          float f[3], float& e) {
     const float r2 = rx * rx + ry * ry + rz * rz;
     float fs;
-    if (p.td_kind == MAFM_PAIR_LJ) {
+    if (w.td_kind == MAFM_PAIR_LJ) {
         const float ir2 = rcp_nr(r2);
         const float ir6 = ir2 * ir2 * ir2;
-        const float t6 = (float)p.td_p[0] * ir6;
-        const float t12 = (float)p.td_p[1] * ir6 * ir6;
+        const float t6 = w.td_p0 * ir6;
+        const float t12 = w.td_p1 * ir6 * ir6;
         e = t12 - t6;
         fs = fmaf(12.f, t12, -6.f * t6) * ir2;
     } else {
         const float ir = rsqrt_fast(r2);
         const float r = r2 * ir;
-        const float d = __expf(-(float)p.td_p[1] * (r - (float)p.td_p[2]));
+        const float d = __expf(-w.td_p1 * (r - w.td_p2));
         const float dm1 = d - 1.f;
-        e = (float)p.td_p[0] * dm1 * dm1;
-        fs = 2.f * (float)p.td_p[0] * (float)p.td_p[1] * d * dm1 * ir;
+        e = w.td_p0 * dm1 * dm1;
+        fs = 2.f * w.td_p0 * w.td_p1 * d * dm1 * ir;
     }
-    if (p.td_coul) {
+    if (w.td_coul) {
         const float ir = rsqrt_fast(r2);
-        const float ec = (float)p.td_qq * ir;
+        const float ec = w.td_qq * ir;
         fs = fmaf(ec * ir, ir, fs);
         e += ec;
     }
@@ -267,6 +339,30 @@ __device__ __forceinline__ void td_vdw32(const ScanParams& p, float rx, float ry
     f[1] = fs * ry;
     f[2] = fs * rz;
 }
+
+// double-float helpers
+__device__ __forceinline__ DF df_norm(float s, float c) {
+    const float h = s + c;
+    return DF{h, c - (h - s)};
+}
+
+__device__ __forceinline__ DF df_add2(DF a, DF b) {
+    float s, e;
+    two_sum(a.hi, b.hi, s, e);
+    e += a.lo + b.lo;
+    return df_norm(s, e);
+}
+
+__device__ __forceinline__ DF df_scale(DF a, float k) {   // exact for k a power of two
+    return DF{a.hi * k, a.lo * k};
+}
+
+__device__ __forceinline__ DF df_div6(DF a) {
+    const float q = a.hi / 6.f;
+    const float r = fmaf(-q, 6.f, a.hi);   // exact remainder
+    return df_norm(q, (r + a.lo) / 6.f);
+}
+
 
 __device__ __forceinline__ unsigned long long global_ns() {
     unsigned long long t;
@@ -280,6 +376,7 @@ struct WarpHdr {
     unsigned long long mbar;
     int assign[32];
     int pad[2];
+    WarpParams wp;
 };
 static_assert(sizeof(WarpHdr) % 16 == 0, "warp header keeps the atom slice 16-byte aligned");
 
@@ -351,18 +448,18 @@ struct GroupState {
     int phase;
     int n_tot;        // FIRE / SD step counter
     int nnn;          // FIRE steps since the last P<0
+    int outside;
     float fdt, alpha;
     DF px, py, pz;    // tip
     DF ex, ey, ez;    // evaluation position of this slot
     float vx, vy, vz;
     float ux, uy, uz; // midpoint v2 / rk4 v_k
     float sx, sy, sz; // rk4 sum of velocities
-    float gx, gy, gz; // rk4 sum of forces / midpoint f1 unused
-    double esum;      // rk4 sum of energies
-    double e_last;    // System::energies_[1] of the last step
-    DF dx_, dy_;      // dummy xy
-    double dz64;      // dummy z
-    int outside;
+    float gx, gy, gz; // rk4 sum of forces
+    DF esum;          // rk4 sum of energies
+    DF e_last;        // System::energies_[1] of the last step
+    DF dxy[2];        // dummy x, y
+    DF dzd;           // dummy z
 };
 
 template <int G>
@@ -378,6 +475,7 @@ __global__ void __launch_bounds__(256) relax32_kernel(const BatchScan* __restric
     const size_t slice = sizeof(WarpHdr) + (size_t)smem_terms * sizeof(AtomRec32);
     WarpHdr* hdr = reinterpret_cast<WarpHdr*>(smem_raw + (size_t)warp * slice);
     AtomRec32* sm_terms = reinterpret_cast<AtomRec32*>(hdr + 1);
+    const WarpParams& W = hdr->wp;
 
     if (lane == 0) {
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&hdr->mbar)) : "memory");
@@ -395,6 +493,8 @@ __global__ void __launch_bounds__(256) relax32_kernel(const BatchScan* __restric
     const AtomRec32* terms = nullptr;
     int n_terms = 0;
     bool coul = false;
+    int pairs_per_eval = 0;
+    mafm_point* out = nullptr;
 
     unsigned err = 0;
     unsigned long long my_steps = 0, my_evals = 0, my_pairs = 0;
@@ -414,13 +514,13 @@ __global__ void __launch_bounds__(256) relax32_kernel(const BatchScan* __restric
         return lo;
     };
 
-    auto start_level = [&](const ScanParams& P) {
-        g.fdt = (float)P.dt;
+    auto start_level = [&]() {
+        g.fdt = W.dt0;
         g.alpha = 0.1f;
         g.nnn = 0;
         g.n_tot = 1;
         g.outside = 0;
-        g.phase = P.maxsteps <= 1 ? PH_OUT : PH_EVAL0;
+        g.phase = W.maxsteps <= 1 ? PH_OUT : PH_EVAL0;
         g.ex = g.px; g.ey = g.py; g.ez = g.pz;
     };
 
@@ -430,16 +530,15 @@ __global__ void __launch_bounds__(256) relax32_kernel(const BatchScan* __restric
         const int i = c / P.ny, j = c % P.ny;
         double x, y;
         dummy_xy(P, P.tip_pbc && P.ts_mode != 2, i * P.dx, j * P.dy, x, y);
-        g.dx_ = df_split(x);
-        g.dy_ = df_split(y);
-        g.dz64 = P.zhigh;
-        g.px = g.dx_;
-        g.py = g.dy_;
+        g.dxy[0] = df_split(x);
+        g.dxy[1] = df_split(y);
+        g.dzd = df_split(P.zhigh);
+        g.px = g.dxy[0];
+        g.py = g.dxy[1];
         g.pz = df_split(P.zhigh - P.tip_dummy_d);
         g.vx = g.vy = g.vz = 0.f;
-        g.e_last = 0.0;
-        g.k = 0;
-        start_level(P);
+        g.e_last = DF{0.f, 0.f};
+        start_level();
     };
 
     // Watchdog: a warp that runs longer than watchdog_ns stops with ERR_WATCHDOG
@@ -509,6 +608,11 @@ __global__ void __launch_bounds__(256) relax32_kernel(const BatchScan* __restric
                 pending = -1;
                 n_terms = B.p.n_terms_direct;
                 coul = B.has_coulomb != 0;
+                pairs_per_eval = B.n_pairs_per_eval;
+                out = B.out;
+                __syncwarp();
+                if (lane == 0) make_warp_params(B, hdr->wp);
+                __syncwarp();
                 if (n_terms > 0 && n_terms <= smem_terms) {
                     if (!stage_terms(hdr, sm_terms, B.p.atoms32, n_terms, phase, lane)) {
                         err |= ERR_STAGE_TIMEOUT;
@@ -529,7 +633,6 @@ __global__ void __launch_bounds__(256) relax32_kernel(const BatchScan* __restric
         }
         if (!alive) break;
 
-        const ScanParams& P = S->p;
         const bool working = g.col >= 0;
 
         // ---------------- one force evaluation per group ----------------
@@ -556,33 +659,32 @@ __global__ void __launch_bounds__(256) relax32_kernel(const BatchScan* __restric
         if (G > 1) acc.template group_reduce<G>();
 
         if (working) {
-            float v[4] = {0.f, 0.f, 0.f, 0.f};
-            if (P.ts_mode == 1) {
-                float qx, qy, qz;
-                rel_origin(P.es, g.ex, g.ey, g.ez, qx, qy, qz);
-                int unused = 0;
-                interp32(P.es, qx, qy, qz, v, unused, err);
-            } else if (P.ts_mode == 2) {
-                float qx, qy, qz;
-                rel_origin(P.grid, g.ex, g.ey, g.ez, qx, qy, qz);
-                interp32(P.grid, qx, qy, qz, v, g.outside, err);
+            const int mode = W.ts_mode;
+            if (mode != 0) {
+                float v[4] = {0.f, 0.f, 0.f, 0.f};
+                if (mode == 1) {
+                    int unused = 0;
+                    interp32(W.es, g.ex, g.ey, g.ez, v, unused, err);
+                } else {
+                    interp32(W.grid, g.ex, g.ey, g.ez, v, g.outside, err);
+                }
+                acc.add(v);
             }
-            if (P.ts_mode != 0) acc.add(v);
             my_evals += (lg == 0);
-            my_pairs += (lg == 0) ? (unsigned long long)S->n_pairs_per_eval : 0ull;
-
-            const float Fsx = acc.s[0] + acc.c[0], Fsy = acc.s[1] + acc.c[1], Fsz = acc.s[2] + acc.c[2];
-            const double Es = (double)acc.s[3] + (double)acc.c[3];
+            my_pairs += (lg == 0) ? (unsigned long long)pairs_per_eval : 0ull;
 
             if (g.phase == PH_OUT) {
                 // Output record of this level (System::getOutput).
                 const int n = g.n_tot;
-                int st = (n >= P.maxsteps ? MAFM_PT_MAXSTEPS : 0) | (g.outside ? MAFM_PT_OUTSIDE : 0);
-                const double Fx = (double)acc.s[0] + (double)acc.c[0];
-                const double Fy = (double)acc.s[1] + (double)acc.c[1];
-                const double Fz = (double)acc.s[2] + (double)acc.c[2];
-                if (!isfinite(Fx) || !isfinite(Fy) || !isfinite(Fz) || !isfinite(Es)) st |= MAFM_PT_NONFINITE;
+                const int nz = W.nz;
+                int st = (n >= W.maxsteps ? MAFM_PT_MAXSTEPS : 0) | (g.outside ? MAFM_PT_OUTSIDE : 0);
                 if (lg == 0) {
+                    const double Fx = (double)acc.s[0] - (double)acc.c[0];
+                    const double Fy = (double)acc.s[1] - (double)acc.c[1];
+                    const double Fz = (double)acc.s[2] - (double)acc.c[2];
+                    const double Es = (double)acc.s[3] - (double)acc.c[3];
+                    if (!isfinite(Fx) || !isfinite(Fy) || !isfinite(Fz) || !isfinite(Es))
+                        st |= MAFM_PT_NONFINITE;
                     mafm_point r;
                     r.tip[0] = df_val(g.px);
                     r.tip[1] = df_val(g.py);
@@ -593,71 +695,69 @@ __global__ void __launch_bounds__(256) relax32_kernel(const BatchScan* __restric
                     r.energy = Es;
                     r.steps = n;
                     r.status = st;
-                    S->out[(size_t)(g.col - S->col_begin) * P.nz + g.k] = r;
+                    out[(size_t)(g.col - W.col_begin) * nz + g.k] = r;
                     my_steps += (unsigned long long)n;
                     status_or |= (unsigned)st;
                 }
                 // System::lowerTip (system.hpp:51-54)
-                g.dz64 -= P.dz;
-                {
-                    const DF dzs = df_split(-P.dz);
-                    DF z = df_add(g.pz, dzs.hi);
-                    g.pz = df_add(z, dzs.lo);
-                }
+                const DF mdz = DF{-W.dz.hi, -W.dz.lo};
+                g.dzd = df_add2(g.dzd, mdz);
+                g.pz = df_add2(g.pz, mdz);
                 g.k++;
-                if (g.k >= P.nz) g.col = -1;
-                else start_level(P);
+                if (g.k >= nz) g.col = -1;
+                else start_level();
             } else {
                 // Full evaluation: add the tip–dummy coupling (simulation.cpp:503-515).
-                const DF dzf = df_split(g.dz64);
-                const float rx = (g.dx_.hi - g.ex.hi) + (g.dx_.lo - g.ex.lo);
-                const float ry = (g.dy_.hi - g.ey.hi) + (g.dy_.lo - g.ey.lo);
-                const float rz = (dzf.hi - g.ez.hi) + (dzf.lo - g.ez.lo);
+                const float rx = (g.dxy[0].hi - g.ex.hi) + (g.dxy[0].lo - g.ex.lo);
+                const float ry = (g.dxy[1].hi - g.ey.hi) + (g.dxy[1].lo - g.ey.lo);
+                const float rz = (g.dzd.hi - g.ez.hi) + (g.dzd.lo - g.ez.lo);
                 float ftd[3], etd;
-                td_vdw32(P, rx, ry, rz, ftd, etd);
-                // XY spring in FP64 (interactions.cpp:252-266)
-                const double drx = rx, dry = ry;
-                const double rr2 = drx * drx + dry * dry;
-                double eh, hx = 0.0, hy = 0.0;
-                if (P.harm_r0 == 0.0) {
-                    eh = P.harm_k * rr2;
-                    if (rr2 > 1e-20) { hx = -2 * P.harm_k * drx; hy = -2 * P.harm_k * dry; }
+                td_vdw32(W, rx, ry, rz, ftd, etd);
+                // XY spring (interactions.cpp:252-266)
+                const float rr2 = rx * rx + ry * ry;
+                float eh, hx = 0.f, hy = 0.f;
+                if (W.harm_r0 == 0.f) {
+                    eh = W.harm_k * rr2;
+                    if (rr2 > 1e-20f) { hx = -2.f * W.harm_k * rx; hy = -2.f * W.harm_k * ry; }
                 } else {
-                    const double rr = sqrt(rr2);
-                    const double dr = rr - P.harm_r0;
-                    eh = P.harm_k * dr * dr;
-                    if (rr > 1e-10) {
-                        const double s = -2 * P.harm_k * dr / rr;
-                        hx = s * drx;
-                        hy = s * dry;
+                    const float rr = sqrtf(rr2);
+                    const float dr = rr - W.harm_r0;
+                    eh = W.harm_k * dr * dr;
+                    if (rr > 1e-10f) {
+                        const float sc = -2.f * W.harm_k * dr / rr;
+                        hx = sc * rx;
+                        hy = sc * ry;
                     }
                 }
                 float Fx, Fy, Fz;
                 {
                     float t, e;
                     two_sum(acc.s[0], -ftd[0], t, e);
-                    Fx = t + (acc.c[0] + e) - (float)hx;
+                    Fx = t + ((e - acc.c[0]) - hx);
                     two_sum(acc.s[1], -ftd[1], t, e);
-                    Fy = t + (acc.c[1] + e) - (float)hy;
+                    Fy = t + ((e - acc.c[1]) - hy);
                     two_sum(acc.s[2], -ftd[2], t, e);
-                    Fz = t + (acc.c[2] + e);
+                    Fz = t + (e - acc.c[2]);
                 }
-                const double E = Es + (double)etd + eh;
-                (void)Fsx; (void)Fsy; (void)Fsz;
+                // total energy as a double-float: surface sum + dummy terms + spring
+                DF E = df_norm(acc.s[3], -acc.c[3]);
+                E = df_add(E, etd);
+                E = df_add(E, eh);
 
                 bool step_done = false;
                 float SFx = Fx, SFy = Fy, SFz = Fz;
-                double SE = E;
+                DF SE = E;
                 const float dt = g.fdt;
-                if (P.minimiser == MAFM_MIN_SD) {
+                const int integ = W.integrator;
+                if (W.minimiser == MAFM_MIN_SD) {
                     step_done = true;
-                } else if (P.integrator == MAFM_INT_EULER) {
+                } else if (integ == MAFM_INT_EULER) {
                     g.px = df_add(g.px, dt * g.vx);
                     g.py = df_add(g.py, dt * g.vy);
                     g.pz = df_add(g.pz, dt * g.vz);
                     g.vx = fmaf(dt, Fx, g.vx); g.vy = fmaf(dt, Fy, g.vy); g.vz = fmaf(dt, Fz, g.vz);
                     step_done = true;
-                } else if (P.integrator == MAFM_INT_MIDPOINT) {
+                } else if (integ == MAFM_INT_MIDPOINT) {
                     if (g.phase == PH_EVAL0) {
                         const float h = 0.5f * dt;
                         g.ux = fmaf(h, Fx, g.vx); g.uy = fmaf(h, Fy, g.vy); g.uz = fmaf(h, Fz, g.vz);
@@ -682,21 +782,21 @@ __global__ void __launch_bounds__(256) relax32_kernel(const BatchScan* __restric
                         g.phase = PH_EVAL1;
                     } else if (g.phase == PH_EVAL1) {
                         g.gx = fmaf(2.f, Fx, g.gx); g.gy = fmaf(2.f, Fy, g.gy); g.gz = fmaf(2.f, Fz, g.gz);
-                        g.esum += 2.0 * E;
+                        g.esum = df_add2(g.esum, df_scale(E, 2.f));
                         g.sx = fmaf(2.f, g.ux, g.sx); g.sy = fmaf(2.f, g.uy, g.sy); g.sz = fmaf(2.f, g.uz, g.sz);
                         g.ex = df_add(g.px, h * g.ux); g.ey = df_add(g.py, h * g.uy); g.ez = df_add(g.pz, h * g.uz);
                         g.ux = fmaf(h, Fx, g.vx); g.uy = fmaf(h, Fy, g.vy); g.uz = fmaf(h, Fz, g.vz);
                         g.phase = PH_EVAL2;
                     } else if (g.phase == PH_EVAL2) {
                         g.gx = fmaf(2.f, Fx, g.gx); g.gy = fmaf(2.f, Fy, g.gy); g.gz = fmaf(2.f, Fz, g.gz);
-                        g.esum += 2.0 * E;
+                        g.esum = df_add2(g.esum, df_scale(E, 2.f));
                         g.sx = fmaf(2.f, g.ux, g.sx); g.sy = fmaf(2.f, g.uy, g.sy); g.sz = fmaf(2.f, g.uz, g.sz);
                         g.ex = df_add(g.px, dt * g.ux); g.ey = df_add(g.py, dt * g.uy); g.ez = df_add(g.pz, dt * g.uz);
                         g.ux = fmaf(dt, Fx, g.vx); g.uy = fmaf(dt, Fy, g.vy); g.uz = fmaf(dt, Fz, g.vz);
                         g.phase = PH_EVAL3;
                     } else {
                         g.gx += Fx; g.gy += Fy; g.gz += Fz;
-                        g.esum += E;
+                        g.esum = df_add2(g.esum, E);
                         g.sx += g.ux; g.sy += g.uy; g.sz += g.uz;
                         const float s6 = dt / 6.f;
                         g.px = df_add(g.px, s6 * g.sx);
@@ -704,24 +804,25 @@ __global__ void __launch_bounds__(256) relax32_kernel(const BatchScan* __restric
                         g.pz = df_add(g.pz, s6 * g.sz);
                         g.vx = fmaf(s6, g.gx, g.vx); g.vy = fmaf(s6, g.gy, g.vy); g.vz = fmaf(s6, g.gz, g.vz);
                         SFx = g.gx / 6.f; SFy = g.gy / 6.f; SFz = g.gz / 6.f;
-                        SE = g.esum / 6.0;
+                        SE = df_div6(g.esum);
                         step_done = true;
                     }
                 }
                 if (step_done) {
-                    // checkConvergence (minimiser.cpp:15-37)
-                    const double ediff = SE - g.e_last;
+                    // checkConvergence (minimiser.cpp:15-37); the energy change is
+                    // taken between double-float totals
+                    const float ediff = (SE.hi - g.e_last.hi) + (SE.lo - g.e_last.lo);
                     g.e_last = SE;
                     const float fl = sqrtf(SFx * SFx + SFy * SFy + SFz * SFz);
                     bool conv;
-                    if (P.minterm == MAFM_TERM_E) conv = fabs(ediff) < P.etol;
-                    else if (P.minterm == MAFM_TERM_F) conv = fl < (float)P.ftol;
-                    else conv = fabs(ediff) < P.etol && fl < (float)P.ftol;
+                    if (W.minterm == MAFM_TERM_E) conv = fabsf(ediff) < W.etol;
+                    else if (W.minterm == MAFM_TERM_F) conv = fl < W.ftol;
+                    else conv = fabsf(ediff) < W.etol && fl < W.ftol;
                     if (conv) {
                         g.phase = PH_OUT;
                     } else {
-                        if (P.minimiser == MAFM_MIN_SD) {
-                            const float sdt = (float)P.dt;
+                        if (W.minimiser == MAFM_MIN_SD) {
+                            const float sdt = W.dt0;
                             g.px = df_add(g.px, sdt * SFx);
                             g.py = df_add(g.py, sdt * SFy);
                             g.pz = df_add(g.pz, sdt * SFz);
@@ -746,14 +847,14 @@ __global__ void __launch_bounds__(256) relax32_kernel(const BatchScan* __restric
                                 g.alpha = 0.1f;
                             } else {
                                 if (g.nnn > 5) {
-                                    g.fdt = fminf(g.fdt * 1.1f, (float)(10 * P.dt));
+                                    g.fdt = fminf(g.fdt * 1.1f, W.dt_max);
                                     g.alpha *= 0.99f;
                                 }
                                 g.nnn++;
                             }
                         }
                         g.n_tot++;
-                        g.phase = g.n_tot >= P.maxsteps ? PH_OUT : PH_EVAL0;
+                        g.phase = g.n_tot >= W.maxsteps ? PH_OUT : PH_EVAL0;
                     }
                     g.ex = g.px; g.ey = g.py; g.ez = g.pz;
                 }
@@ -791,11 +892,7 @@ __global__ void sample32_kernel(const ScanParams p, int what, const double* pts,
     int outside = 0;
     if (what == 1) {
         float v[4] = {0, 0, 0, 0};
-        if (p.es.g32) {
-            float qx, qy, qz;
-            rel_origin(p.es, x, y, z, qx, qy, qz);
-            interp32(p.es, qx, qy, qz, v, outside, err);
-        }
+        if (p.es.g32) interp32(make_lookup(p.es), x, y, z, v, outside, err);
         acc.add(v);
     } else {
         const bool coul = p.has_coulomb != 0;
@@ -808,18 +905,11 @@ __global__ void sample32_kernel(const ScanParams p, int what, const double* pts,
             acc.add(v);
         }
         float v[4] = {0, 0, 0, 0};
-        if (p.ts_mode == 1) {
-            float qx, qy, qz;
-            rel_origin(p.es, x, y, z, qx, qy, qz);
-            interp32(p.es, qx, qy, qz, v, outside, err);
-        } else if (p.ts_mode == 2) {
-            float qx, qy, qz;
-            rel_origin(p.grid, x, y, z, qx, qy, qz);
-            interp32(p.grid, qx, qy, qz, v, outside, err);
-        }
+        if (p.ts_mode == 1) interp32(make_lookup(p.es), x, y, z, v, outside, err);
+        else if (p.ts_mode == 2) interp32(make_lookup(p.grid), x, y, z, v, outside, err);
         acc.add(v);
     }
-    for (int m = 0; m < 4; ++m) out[4 * i + m] = (double)acc.s[m] + (double)acc.c[m];
+    for (int m = 0; m < 4; ++m) out[4 * i + m] = (double)acc.s[m] - (double)acc.c[m];
     if (err) atomicOr(&ctr->error_word, err);
 }
 
@@ -877,14 +967,11 @@ __global__ void __launch_bounds__(256) grid_build32_kernel(const ScanParams p, c
         if (valid) {
             if (p.es.g32) {
                 float v[4] = {0, 0, 0, 0};
-                float qx, qy, qz;
-                rel_origin(p.es, tx, ty, tz, qx, qy, qz);
                 int unused = 0;
-                interp32(p.es, qx, qy, qz, v, unused, err);
+                interp32(make_lookup(p.es), tx, ty, tz, v, unused, err);
                 acc.add(v);
             }
-            out[idx] = make_float4(acc.s[0] + acc.c[0], acc.s[1] + acc.c[1], acc.s[2] + acc.c[2],
-                                   acc.s[3] + acc.c[3]);
+            out[idx] = make_float4(acc.val(0), acc.val(1), acc.val(2), acc.val(3));
         }
     }
     if (err) atomicOr(&ctr->error_word, err);
