@@ -163,6 +163,7 @@ typedef struct mafm_run_stats {
 
 typedef struct mafm_input mafm_input;   /* parsed input files + prepared System */
 typedef struct mafm_scan mafm_scan;     /* device-resident scan */
+typedef struct mafm_plan mafm_plan;     /* prepared batched launch */
 
 /* ---- errors / version ---------------------------------------------------- */
 const char* mafm_last_error(void);
@@ -230,6 +231,30 @@ int mafm_run_batch(mafm_scan* const* scans, int32_t n_scans, const mafm_run_opts
 #define MAFM_NOALLOC_MAX_SCANS 32
 int mafm_run_batch_noalloc(mafm_scan* const* scans, int32_t n_scans, const mafm_run_opts* opts,
                            mafm_point* const* outs, mafm_run_stats* stats, void* stream);
+
+/* A prepared batched FP32C relaxation (the same persistent launch as
+ * mafm_run_batch) whose per-scan descriptors are uploaded once, so that the
+ * launch itself allocates nothing, never synchronises and can be replayed or
+ * captured in a CUDA graph.  Replaces the pixel loop of Simulation::run
+ * (simulation.cpp:78-122) for many scans at once.  outs must be device memory
+ * and stay valid for the plan's lifetime. */
+int mafm_plan_create(mafm_scan* const* scans, int32_t n_scans, const mafm_run_opts* opts,
+                     mafm_point* const* outs, mafm_plan** out);
+/* Enqueue one relaxation of every scan of the plan on stream. */
+int mafm_plan_launch(mafm_plan* plan, void* stream);
+/* Counters of the last launch; synchronises the stream. */
+int mafm_plan_stats(mafm_plan* plan, mafm_run_stats* stats, void* stream);
+/* The launch shape the plan uses (lanes per column, block, tile). */
+int mafm_plan_config(const mafm_plan* plan, mafm_run_opts* opts);
+int mafm_plan_destroy(mafm_plan* plan);
+
+/* Autotuner: times launch shapes of the FP32C kernel (lanes per column, block
+ * size, columns per warp tile) on the given scans and returns the fastest in
+ * best (pass it to mafm_run / mafm_run_batch / mafm_plan_create).  No
+ * counterpart in the reference, whose OpenMP schedule is fixed (dynamic, 1,
+ * simulation.cpp:78). */
+int mafm_autotune(mafm_scan* const* scans, int32_t n_scans, mafm_run_opts* best, double* best_ms,
+                  void* stream);
 
 /* Evaluate the tip–surface force and energy at n given tip positions
  * (System::evalTipSurfaceForces, system.cpp:41-51): pairs, external field or

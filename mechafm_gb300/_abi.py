@@ -95,6 +95,14 @@ SIGNATURES = {
                                  C.POINTER(_P), C.POINTER(RunStats), _P]),
     "mafm_run_batch_noalloc": (C.c_int, [C.POINTER(_P), C.c_int32, C.POINTER(RunOpts),
                                          C.POINTER(_P), C.POINTER(RunStats), _P]),
+    "mafm_plan_create": (C.c_int, [C.POINTER(_P), C.c_int32, C.POINTER(RunOpts), C.POINTER(_P),
+                                   C.POINTER(_P)]),
+    "mafm_plan_launch": (C.c_int, [_P, _P]),
+    "mafm_plan_stats": (C.c_int, [_P, C.POINTER(RunStats), _P]),
+    "mafm_plan_config": (C.c_int, [_P, C.POINTER(RunOpts)]),
+    "mafm_plan_destroy": (C.c_int, [_P]),
+    "mafm_autotune": (C.c_int, [C.POINTER(_P), C.c_int32, C.POINTER(RunOpts),
+                                C.POINTER(C.c_double), _P]),
     "mafm_scan_sample": (C.c_int, [_P, C.c_int32, C.c_int32, _P, C.c_int64, _P]),
     "mafm_scan_grid_info": (C.c_int, [_P, C.c_int32, C.c_int32 * 3, C.c_double * 9,
                                       C.c_double * 3]),

@@ -145,6 +145,8 @@ struct BatchScan {
     int col_begin, col_end;
     int n_pairs_per_eval;     // vdW + Coulomb terms per force evaluation
     int has_coulomb;
+    const int* order;         // processing order of the columns (most expensive
+                              // first), nullptr = index order; whole scans only
 };
 
 struct Relax32Config {

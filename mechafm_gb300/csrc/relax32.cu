@@ -591,7 +591,7 @@ __global__ void __launch_bounds__(256) relax32_kernel(const BatchScan* __restric
                 exhausted = __shfl_sync(kFull, (int)exhausted, 0) != 0;
                 if (g.col == -1) {
                     const int a = hdr->assign[grp];
-                    if (a >= 0) start_column(S->p, a);
+                    if (a >= 0) start_column(S->p, S->order ? __ldg(S->order + a) : a);
                     else if (a == -2) g.col = -2;
                 }
                 __syncwarp();

@@ -175,6 +175,23 @@ __global__ void nodes_to_float4(const Node64* in, float4* out, long long n) {
 
 __global__ void write_batch(BatchScan* dst, BatchScan v) { *dst = v; }
 
+// Expected relaxation cost of each pixel column: the density of tip–atom terms
+// under the pixel (Gaussian of 2 A in xy).  Columns over the molecule take up
+// to ten times more FIRE steps than columns over vacuum; running the
+// expensive ones first shortens the tail of the persistent launch.
+__global__ void column_cost_proxy(const AtomRec32* terms, int n_terms, int nx, int ny, double dx,
+                                  double dy, float* w) {
+    const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= (long long)nx * ny) return;
+    const float x = (float)((c / ny) * dx), y = (float)((c % ny) * dy);
+    float acc = 0.f;
+    for (int t = 0; t < n_terms; ++t) {
+        const float ex = x - terms[t].a.x, ey = y - terms[t].a.y;
+        acc += __expf(-(ex * ex + ey * ey) * 0.125f);
+    }
+    w[c] = acc;
+}
+
 unsigned grid_blocks(long long n) {
     long long b = (n + 255) / 256;
     const long long cap = (long long)sm_count() * 32;
@@ -197,6 +214,8 @@ struct mafm_scan {
     mafm::DevBuf<mafm::RunCounters> ctr;
     mafm::DevBuf<mafm::BatchScan> batch;
     mafm::DevBuf<mafm_point> stage;
+    mafm::DevBuf<int> order;             // columns by descending expected cost
+    bool order_built = false;
     mafm::RunCounters* host_ctr = nullptr;   // pinned
     int n_pairs_per_eval = 0;
     int has_coulomb = 0;
@@ -481,6 +500,42 @@ void ensure_grid(mafm_scan& s, bool fp64, cudaStream_t st) {
     s.P.grid = s.grid_view;
 }
 
+// Cost-ordered schedule of a scan's columns, built once: proxy on the GPU,
+// counting sort into 1024 buckets (descending) on the host.
+void ensure_order(mafm_scan& s, cudaStream_t st) {
+    if (s.order_built) return;
+    s.order_built = true;
+    const long long n = (long long)s.d.nx * s.d.ny;
+    if (s.d.rigidgrid || s.P.n_terms == 0 || n < 2) return;
+    DevBuf<float> w;
+    w.alloc((size_t)n);
+    column_cost_proxy<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(s.atoms32.p, s.P.n_terms, s.d.nx,
+                                                                  s.d.ny, s.d.dx, s.d.dy, w.p);
+    cuda_check(cudaGetLastError(), "cost proxy");
+    std::vector<float> hw((size_t)n);
+    cuda_check(cudaMemcpyAsync(hw.data(), w.p, (size_t)n * sizeof(float), cudaMemcpyDeviceToHost, st),
+               "cost proxy");
+    cuda_check(cudaStreamSynchronize(st), "cost proxy");
+    float wmax = 0.f;
+    for (float v : hw) wmax = std::max(wmax, v);
+    constexpr int kBuckets = 1024;
+    std::vector<int> count(kBuckets + 1, 0);
+    std::vector<int> bucket((size_t)n);
+    for (long long c = 0; c < n; ++c) {
+        int b = wmax > 0.f ? (int)((1.f - hw[c] / wmax) * (kBuckets - 1)) : 0;
+        b = std::min(std::max(b, 0), kBuckets - 1);
+        bucket[c] = b;
+        count[b + 1]++;
+    }
+    for (int b = 0; b < kBuckets; ++b) count[b + 1] += count[b];
+    std::vector<int> ord((size_t)n);
+    for (long long c = 0; c < n; ++c) ord[count[bucket[c]]++] = (int)c;
+    s.order.alloc((size_t)n);
+    cuda_check(cudaMemcpyAsync(s.order.p, ord.data(), (size_t)n * sizeof(int), cudaMemcpyHostToDevice, st),
+               "upload order");
+    cuda_check(cudaStreamSynchronize(st), "upload order");
+}
+
 bool is_device_ptr(const void* p) {
     cudaPointerAttributes a{};
     if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
@@ -643,6 +698,10 @@ int mafm_run(mafm_scan* scan, const mafm_run_opts* opts, mafm_point* out, mafm_r
             b.col_end = ce;
             b.n_pairs_per_eval = scan->n_pairs_per_eval;
             b.has_coulomb = scan->has_coulomb;
+            if (cb == 0 && ce == n_cols_all) {
+                ensure_order(*scan, st);
+                b.order = scan->order.p;
+            }
             write_batch<<<1, 1, 0, st>>>(scan->batch.p, b);
             const Relax32Config cfg = default_config(ce - cb, b.p.n_terms_direct, opts);
             const long long n_tiles = ((long long)(ce - cb) + cfg.cols_per_tile - 1) / cfg.cols_per_tile;
@@ -701,6 +760,7 @@ int mafm_run_batch(mafm_scan* const* scans, int32_t n_scans, const mafm_run_opts
             max_cols = std::max(max_cols, cols);
             total_cols += cols;
             ensure_grid(*s, false, st);
+            ensure_order(*s, st);
             max_terms = std::max(max_terms, s->d.rigidgrid ? 0 : s->P.n_terms);
         }
         Relax32Config cfg = default_config(total_cols, max_terms, opts);
@@ -716,6 +776,7 @@ int mafm_run_batch(mafm_scan* const* scans, int32_t n_scans, const mafm_run_opts
             b.col_end = s->d.nx * s->d.ny;
             b.n_pairs_per_eval = s->n_pairs_per_eval;
             b.has_coulomb = s->has_coulomb;
+            b.order = s->order.p;
             tiles += ((long long)b.col_end + cfg.cols_per_tile - 1) / cfg.cols_per_tile;
         }
         DevBuf<BatchScan> dbs;
@@ -828,6 +889,7 @@ BatchScan scan_batch_entry(const mafm_scan* s, mafm_point* out) {
     b.col_end = s->d.nx * s->d.ny;
     b.n_pairs_per_eval = s->n_pairs_per_eval;
     b.has_coulomb = s->has_coulomb;
+    b.order = s->order_built ? s->order.p : nullptr;
     return b;
 }
 
@@ -838,3 +900,205 @@ Relax32Config relax32_config(long long n_cols, int max_terms, const mafm_run_opt
 void check_run_errors(const RunCounters& c) { check_device_errors(c); }
 
 }  // namespace mafm
+
+// ---- batch plans and the autotuner -----------------------------------------
+
+struct mafm_plan {
+    int device = 0;
+    int n_scans = 0;
+    long long tiles = 0;
+    mafm::Relax32Config cfg{};
+    mafm::DevBuf<mafm::BatchScan> list;
+    mafm::DevBuf<mafm::RunCounters> ctr;
+    mafm::RunCounters* host_ctr = nullptr;
+    ~mafm_plan() {
+        if (host_ctr) cudaFreeHost(host_ctr);
+    }
+};
+
+namespace mafm {
+namespace {
+
+// Descriptor list of a batch (tile numbering for the persistent kernel).
+std::vector<BatchScan> batch_entries(mafm_scan* const* scans, int n, mafm_point* const* outs,
+                                     const Relax32Config& cfg, long long& tiles) {
+    std::vector<BatchScan> bs((size_t)n);
+    tiles = 0;
+    for (int i = 0; i < n; ++i) {
+        bs[i] = scan_batch_entry(scans[i], outs[i]);
+        bs[i].tile_begin = tiles;
+        tiles += ((long long)bs[i].col_end + cfg.cols_per_tile - 1) / cfg.cols_per_tile;
+    }
+    return bs;
+}
+
+void plan_build(mafm_plan& p, mafm_scan* const* scans, int n, const mafm_run_opts* opts,
+                mafm_point* const* outs, cudaStream_t st) {
+    if (!scans || !outs || n <= 0) fail(MAFM_E_INVALID, "empty batch");
+    if (opts && opts->precision != MAFM_FP32C) fail(MAFM_E_UNSUPPORTED, "plans run MAFM_FP32C");
+    if (opts && (opts->col_begin || opts->col_end)) fail(MAFM_E_INVALID, "plans relax whole scans");
+    p.device = scans[0]->device;
+    cuda_check(cudaSetDevice(p.device), "cudaSetDevice");
+    long long cols = 0;
+    int max_terms = 0;
+    for (int i = 0; i < n; ++i) {
+        if (!scans[i] || !outs[i]) fail(MAFM_E_INVALID, "null scan or output %d", i);
+        if (scans[i]->device != p.device) fail(MAFM_E_INVALID, "scans of one plan must share a device");
+        if (!is_device_ptr(outs[i])) fail(MAFM_E_INVALID, "plan outputs must be device memory");
+        ensure_grid(*scans[i], false, st);
+        ensure_order(*scans[i], st);
+        cols += (long long)scans[i]->d.nx * scans[i]->d.ny;
+        max_terms = std::max(max_terms, scan_direct_terms(scans[i]));
+    }
+    p.cfg = default_config(cols, max_terms, opts);
+    std::vector<BatchScan> bs = batch_entries(scans, n, outs, p.cfg, p.tiles);
+    p.n_scans = n;
+    p.list.alloc(bs.size());
+    p.ctr.alloc(1);
+    cuda_check(cudaMemcpyAsync(p.list.p, bs.data(), bs.size() * sizeof(BatchScan),
+                               cudaMemcpyHostToDevice, st), "upload plan");
+    cuda_check(cudaStreamSynchronize(st), "upload plan");
+    if (!p.host_ctr) cuda_check(cudaMallocHost(&p.host_ctr, sizeof(RunCounters)), "cudaMallocHost");
+}
+
+void plan_launch(mafm_plan& p, cudaStream_t st) {
+    cuda_check(cudaMemsetAsync(p.ctr.p, 0, sizeof(RunCounters), st), "reset counters");
+    cuda_check(launch_relax32(p.list.p, p.n_scans, p.tiles, p.cfg, p.ctr.p, st), "relax32 launch");
+}
+
+}  // namespace
+}  // namespace mafm
+
+extern "C" {
+
+int mafm_plan_create(mafm_scan* const* scans, int32_t n_scans, const mafm_run_opts* opts,
+                     mafm_point* const* outs, mafm_plan** out) {
+    return guarded([&] {
+        if (!out) fail(MAFM_E_INVALID, "null output handle");
+        *out = nullptr;
+        auto* p = new mafm_plan();
+        try {
+            plan_build(*p, scans, n_scans, opts, outs, nullptr);
+        } catch (...) {
+            delete p;
+            throw;
+        }
+        *out = p;
+    });
+}
+
+int mafm_plan_launch(mafm_plan* plan, void* stream) {
+    return guarded([&] {
+        if (!plan) fail(MAFM_E_INVALID, "null plan");
+        plan_launch(*plan, (cudaStream_t)stream);
+    });
+}
+
+int mafm_plan_stats(mafm_plan* plan, mafm_run_stats* stats, void* stream) {
+    return guarded([&] {
+        if (!plan || !stats) fail(MAFM_E_INVALID, "null argument");
+        cudaStream_t st = (cudaStream_t)stream;
+        cuda_check(cudaMemcpyAsync(plan->host_ctr, plan->ctr.p, sizeof(RunCounters),
+                                   cudaMemcpyDeviceToHost, st), "copy counters");
+        cuda_check(cudaStreamSynchronize(st), "plan");
+        const RunCounters c = *plan->host_ctr;
+        *stats = mafm_run_stats{};
+        stats->total_steps = c.total_steps;
+        stats->force_evals = c.force_evals;
+        stats->pair_evals = c.pair_evals;
+        stats->error_word = c.error_word;
+        check_device_errors(c);
+    });
+}
+
+int mafm_plan_destroy(mafm_plan* plan) {
+    if (plan) {
+        cudaSetDevice(plan->device);
+        delete plan;
+    }
+    return MAFM_OK;
+}
+
+int mafm_plan_config(const mafm_plan* plan, mafm_run_opts* opts) {
+    return guarded([&] {
+        if (!plan || !opts) fail(MAFM_E_INVALID, "null argument");
+        *opts = mafm_run_opts{};
+        opts->precision = MAFM_FP32C;
+        opts->lanes_per_column = plan->cfg.lanes;
+        opts->block_threads = plan->cfg.block;
+        opts->columns_per_tile = plan->cfg.cols_per_tile;
+    });
+}
+
+// Time launch shapes on the scans themselves and keep the fastest: lanes per
+// column first (block 256, one column per group per tile), then block size and
+// tile length around the best lane count.
+int mafm_autotune(mafm_scan* const* scans, int32_t n_scans, mafm_run_opts* best, double* best_ms,
+                  void* stream) {
+    return guarded([&] {
+        if (!scans || n_scans <= 0 || !best) fail(MAFM_E_INVALID, "empty batch");
+        cudaStream_t st = (cudaStream_t)stream;
+        cuda_check(cudaSetDevice(scans[0]->device), "cudaSetDevice");
+        size_t total = 0;
+        int max_terms = 0;
+        for (int i = 0; i < n_scans; ++i) {
+            if (!scans[i]) fail(MAFM_E_INVALID, "null scan %d", i);
+            total += (size_t)scans[i]->d.nx * scans[i]->d.ny * scans[i]->d.nz;
+            max_terms = std::max(max_terms, scan_direct_terms(scans[i]));
+        }
+        DevBuf<mafm_point> buf;
+        buf.alloc(total);
+        std::vector<mafm_point*> outs((size_t)n_scans);
+        size_t off = 0;
+        for (int i = 0; i < n_scans; ++i) {
+            outs[i] = buf.p + off;
+            off += (size_t)scans[i]->d.nx * scans[i]->d.ny * scans[i]->d.nz;
+        }
+        cudaEvent_t e0, e1;
+        cuda_check(cudaEventCreate(&e0), "cudaEventCreate");
+        cuda_check(cudaEventCreate(&e1), "cudaEventCreate");
+        struct EvGuard { cudaEvent_t a, b; ~EvGuard() { cudaEventDestroy(a); cudaEventDestroy(b); } } eg{e0, e1};
+        auto time_opts = [&](const mafm_run_opts& o) {
+            mafm_plan p;
+            plan_build(p, scans, n_scans, &o, outs.data(), st);
+            plan_launch(p, st);   // warm-up: module load, attributes
+            cuda_check(cudaEventRecord(e0, st), "cudaEventRecord");
+            plan_launch(p, st);
+            cuda_check(cudaEventRecord(e1, st), "cudaEventRecord");
+            cuda_check(cudaEventSynchronize(e1), "autotune");
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, e0, e1);
+            cuda_check(cudaMemcpy(p.host_ctr, p.ctr.p, sizeof(RunCounters), cudaMemcpyDeviceToHost), "counters");
+            check_device_errors(*p.host_ctr);
+            return (double)ms;
+        };
+        mafm_run_opts o{};
+        o.precision = MAFM_FP32C;
+        o.block_threads = 256;
+        mafm_run_opts keep = o;
+        double keep_ms = 1e300;
+        const int lane_set[6] = {1, 2, 4, 8, 16, 32};
+        for (int G : lane_set) {
+            if (G > 1 && G > std::max(max_terms, 1)) break;
+            o.lanes_per_column = G;
+            o.columns_per_tile = 32 / G;
+            const double ms = time_opts(o);
+            if (ms < keep_ms) { keep_ms = ms; keep = o; }
+        }
+        mafm_run_opts base = keep;
+        for (int block : {128, 256}) {
+            for (int mult : {1, 4}) {
+                mafm_run_opts c = base;
+                c.block_threads = block;
+                c.columns_per_tile = (32 / base.lanes_per_column) * mult;
+                if (block == base.block_threads && c.columns_per_tile == base.columns_per_tile) continue;
+                const double ms = time_opts(c);
+                if (ms < keep_ms) { keep_ms = ms; keep = c; }
+            }
+        }
+        *best = keep;
+        if (best_ms) *best_ms = keep_ms;
+    });
+}
+
+}  // extern "C"

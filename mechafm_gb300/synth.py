@@ -219,26 +219,39 @@ def gaussian_potential(pos: np.ndarray, q: np.ndarray, cell: np.ndarray, n: tupl
                        width: float = 0.5) -> np.ndarray:
     """Periodic potential (Hartree/e) of Gaussian charges on a neutralising background.
 
-    Solves the Poisson equation by FFT on the orthorhombic cell: V(k) =
-    4 pi rho(k) / k^2 with V(0) = 0 (the background), in e/A, then converts
-    e/A -> Hartree/e (1 e/A = BOHR Hartree).
+    The charges are splatted onto the voxel grid as normalised Gaussians
+    (periodic wrap, +-4 widths), then the Poisson equation is solved by FFT on
+    the orthorhombic cell: V(k) = 4 pi rho(k) / k^2 with V(0) = 0 (the
+    background), in e/A, converted e/A -> Hartree/e (1 e/A = BOHR Hartree).
     """
     n0, n1, n2 = n
     L = np.array([cell[0][0], cell[1][1], cell[2][2]])
-    k0 = 2 * np.pi * np.fft.fftfreq(n0, d=L[0] / n0)
-    k1 = 2 * np.pi * np.fft.fftfreq(n1, d=L[1] / n1)
-    k2 = 2 * np.pi * np.fft.fftfreq(n2, d=L[2] / n2)
-    K0, K1, K2 = np.meshgrid(k0, k1, k2, indexing="ij")
-    k2sum = K0 ** 2 + K1 ** 2 + K2 ** 2
-    # structure factor of point charges times the Gaussian form factor
-    rho_k = np.zeros((n0, n1, n2), dtype=np.complex128)
+    h = L / np.array(n)
+    rho = np.zeros((n0, n1, n2))
+    half = [int(math.ceil(4 * width / h[a])) for a in range(3)]
+    offs = [np.arange(-half[a], half[a] + 1) for a in range(3)]
     for a in range(len(q)):
-        rho_k += q[a] * np.exp(-1j * (K0 * pos[a, 0] + K1 * pos[a, 1] + K2 * pos[a, 2]))
-    rho_k *= np.exp(-0.5 * width ** 2 * k2sum)
-    vol = L.prod()
+        idx, wts = [], []
+        for d in range(3):
+            c = pos[a, d] / h[d]
+            i0 = int(math.floor(c))
+            ii = i0 + offs[d]
+            r = (ii - c) * h[d]
+            idx.append(np.mod(ii, n[d]))
+            wts.append(np.exp(-0.5 * (r / width) ** 2))
+        block = q[a] * wts[0][:, None, None] * wts[1][None, :, None] * wts[2][None, None, :]
+        rho[np.ix_(idx[0], idx[1], idx[2])] += block
+    # normalise each Gaussian's discrete sum to its charge
+    norm = (np.sqrt(2 * np.pi) * width) ** 3 / h.prod()
+    rho /= norm * h.prod()
+    k0 = 2 * np.pi * np.fft.fftfreq(n0, d=h[0])
+    k1 = 2 * np.pi * np.fft.fftfreq(n1, d=h[1])
+    k2 = 2 * np.pi * np.fft.rfftfreq(n2, d=h[2])
+    K2 = k0[:, None, None] ** 2 + k1[None, :, None] ** 2 + k2[None, None, :] ** 2
+    rho_k = np.fft.rfftn(rho)
     with np.errstate(divide="ignore", invalid="ignore"):
-        v_k = np.where(k2sum > 0, 4 * np.pi * rho_k / (k2sum * vol), 0.0)
-    v = np.real(np.fft.ifftn(v_k)) * (n0 * n1 * n2)
+        v_k = np.where(K2 > 0, 4 * np.pi * rho_k / K2, 0.0)
+    v = np.fft.irfftn(v_k, s=(n0, n1, n2))
     return v * BOHR
 
 
