@@ -256,6 +256,24 @@ int mafm_plan_destroy(mafm_plan* plan);
 int mafm_autotune(mafm_scan* const* scans, int32_t n_scans, mafm_run_opts* best, double* best_ms,
                   void* stream);
 
+/* Gradients of a scalar loss L of the Fz image (no counterpart in the
+ * reference, which has no derivatives).  Given the relaxed points of a run
+ * (the checkpoint of every z-slice) and w_p = dL/dFz_p per point, the
+ * gradient is taken by implicit differentiation at each relaxed tip position:
+ * J = dF_total/dx (3x3) and dx/dtheta = -J^-1 dF_ts/dtheta, without
+ * unrolling FIRE.  theta: surface atom positions as in the descriptor, the
+ * per-type tip pair parameters tip_pair[t].p (LJ es6, es12; Morse De, a, re)
+ * and the atom charges.  pts and dl_dfz (n_points each) may be host or device
+ * memory; out arrays are host memory (any may be NULL).  Pair and external
+ * field scans only (MAFM_E_UNSUPPORTED for rigid grids). */
+typedef struct mafm_grad {
+    double* dpos;      /* [n_atoms*3] */
+    double* dcharge;   /* [n_atoms] */
+    double* dpair;     /* [n_types*3] */
+} mafm_grad;
+int mafm_adjoint(mafm_scan* scan, const mafm_point* pts, const double* dl_dfz, mafm_grad* out,
+                 void* stream);
+
 /* Evaluate the tip–surface force and energy at n given tip positions
  * (System::evalTipSurfaceForces, system.cpp:41-51): pairs, external field or
  * rigid grid, whatever the scan uses.  what: 0 = all tip–surface terms,

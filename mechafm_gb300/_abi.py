@@ -77,6 +77,11 @@ class RunStats(C.Structure):
                 ("reserved", C.c_uint32), ("kernel_ms", C.c_double)]
 
 
+class Grad(C.Structure):
+    _fields_ = [("dpos", C.POINTER(C.c_double)), ("dcharge", C.POINTER(C.c_double)),
+                ("dpair", C.POINTER(C.c_double))]
+
+
 # Every symbol the header declares, with its ctypes signature.
 _P = C.c_void_p
 SIGNATURES = {
@@ -103,6 +108,7 @@ SIGNATURES = {
     "mafm_plan_destroy": (C.c_int, [_P]),
     "mafm_autotune": (C.c_int, [C.POINTER(_P), C.c_int32, C.POINTER(RunOpts),
                                 C.POINTER(C.c_double), _P]),
+    "mafm_adjoint": (C.c_int, [_P, _P, _P, C.POINTER(Grad), _P]),
     "mafm_scan_sample": (C.c_int, [_P, C.c_int32, C.c_int32, _P, C.c_int64, _P]),
     "mafm_scan_grid_info": (C.c_int, [_P, C.c_int32, C.c_int32 * 3, C.c_double * 9,
                                       C.c_double * 3]),

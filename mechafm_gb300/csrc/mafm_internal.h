@@ -165,6 +165,9 @@ cudaError_t launch_sample32(const ScanParams& p, int what, const double* pts, in
 cudaError_t launch_grid_build32(const ScanParams& p, const GridView& g, float4* out,
                                 RunCounters* ctr, cudaStream_t s);
 int sm_count();
+cudaError_t launch_adjoint(const ScanParams& p, const mafm_point* pts, const double* w,
+                           long long n_points, double qbase_qtip, double* gterm, RunCounters* ctr,
+                           cudaStream_t s);
 
 }  // namespace mafm
 

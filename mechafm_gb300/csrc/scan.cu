@@ -219,6 +219,7 @@ struct mafm_scan {
     mafm::RunCounters* host_ctr = nullptr;   // pinned
     int n_pairs_per_eval = 0;
     int has_coulomb = 0;
+    std::vector<int32_t> atom_type;      // type index of each surface atom (adjoint folding)
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     ~mafm_scan() {
         if (host_ctr) cudaFreeHost(host_ctr);
@@ -598,6 +599,7 @@ int mafm_scan_create(int device, const mafm_scan_desc* desc, mafm_scan** out) {
             s->d.type = nullptr;
             s->d.tip_pair = nullptr;
             s->d.epot = nullptr;
+            s->atom_type.assign(d.type, d.type + d.n_atoms);
             ScanParams& P = s->P;
             std::memset(&P, 0, sizeof P);
             pack_terms(*s, d);
@@ -1102,3 +1104,59 @@ int mafm_autotune(mafm_scan* const* scans, int32_t n_scans, mafm_run_opts* best,
 }
 
 }  // extern "C"
+
+extern "C" int mafm_adjoint(mafm_scan* scan, const mafm_point* pts, const double* dl_dfz,
+                            mafm_grad* out, void* stream) {
+    return guarded([&] {
+        if (!scan || !pts || !dl_dfz || !out) fail(MAFM_E_INVALID, "null argument");
+        if (scan->d.rigidgrid)
+            fail(MAFM_E_UNSUPPORTED, "gradients through a rigid force grid are not provided");
+        cuda_check(cudaSetDevice(scan->device), "cudaSetDevice");
+        cudaStream_t st = (cudaStream_t)stream;
+        const long long npts = (long long)scan->d.nx * scan->d.ny * scan->d.nz;
+        DevBuf<mafm_point> dpts;
+        DevBuf<double> dw, gterm;
+        const mafm_point* pp = pts;
+        const double* pw = dl_dfz;
+        if (!is_device_ptr(pts)) {
+            dpts.alloc((size_t)npts);
+            cuda_check(cudaMemcpyAsync(dpts.p, pts, npts * sizeof(mafm_point), cudaMemcpyHostToDevice, st),
+                       "upload points");
+            pp = dpts.p;
+        }
+        if (!is_device_ptr(dl_dfz)) {
+            dw.alloc((size_t)npts);
+            cuda_check(cudaMemcpyAsync(dw.p, dl_dfz, npts * sizeof(double), cudaMemcpyHostToDevice, st),
+                       "upload weights");
+            pw = dw.p;
+        }
+        const int nt = scan->P.n_terms;
+        gterm.alloc((size_t)std::max(nt, 1) * 7);
+        cuda_check(cudaMemsetAsync(gterm.p, 0, (size_t)std::max(nt, 1) * 7 * sizeof(double), st), "memset");
+        zero_counters(*scan, st);
+        ScanParams p = build_params(*scan);
+        cuda_check(launch_adjoint(p, pp, pw, npts, scan->d.qbase * scan->d.tip_charge, gterm.p,
+                                  scan->ctr.p, st), "adjoint launch");
+        std::vector<double> g((size_t)std::max(nt, 1) * 7);
+        cuda_check(cudaMemcpyAsync(g.data(), gterm.p, g.size() * sizeof(double), cudaMemcpyDeviceToHost, st),
+                   "download gradients");
+        cuda_check(cudaMemcpyAsync(scan->host_ctr, scan->ctr.p, sizeof(RunCounters), cudaMemcpyDeviceToHost, st),
+                   "counters");
+        cuda_check(cudaStreamSynchronize(st), "adjoint");
+        if (scan->host_ctr->error_word & MAFM_PT_NONFINITE)
+            fail(MAFM_E_DEVICE, "singular force Jacobian at a relaxed point");
+        const int na = scan->d.n_atoms, ntypes = scan->d.n_types;
+        if (out->dpos) std::memset(out->dpos, 0, sizeof(double) * 3 * na);
+        if (out->dcharge) std::memset(out->dcharge, 0, sizeof(double) * na);
+        if (out->dpair) std::memset(out->dpair, 0, sizeof(double) * 3 * ntypes);
+        for (int t = 0; t < nt; ++t) {
+            const int a = t % na;
+            const double* v = g.data() + (size_t)t * 7;
+            if (out->dpos)
+                for (int k = 0; k < 3; ++k) out->dpos[3 * a + k] += v[k];
+            if (out->dpair)
+                for (int k = 0; k < 3; ++k) out->dpair[3 * scan->atom_type[a] + k] += v[3 + k];
+            if (out->dcharge) out->dcharge[a] += v[6];
+        }
+    });
+}

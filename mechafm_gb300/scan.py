@@ -67,6 +67,32 @@ class Desc:
         self.c = c
         self._keep = keep
 
+    def with_terms(self, pos: np.ndarray, charge: np.ndarray, pair: np.ndarray) -> "Desc":
+        """A copy of this descriptor with new atom positions (n, 3), charges (n,)
+        and tip pair parameters (n_types, 3); the copy owns those arrays."""
+        c = _abi.ScanDesc()
+        C.pointer(c)[0] = self.c
+        n, nt = self.c.n_atoms, self.c.n_types
+        pos = np.ascontiguousarray(pos, dtype=np.float64).reshape(n, 3)
+        charge = np.ascontiguousarray(charge, dtype=np.float64).reshape(n)
+        pair = np.ascontiguousarray(pair, dtype=np.float64).reshape(nt, 3)
+        pairs = (_abi.Pair * max(nt, 1))()
+        for t in range(nt):
+            pairs[t].kind = self.c.tip_pair[t].kind
+            for m in range(3):
+                pairs[t].p[m] = pair[t, m]
+        c.pos = pos.ctypes.data_as(C.POINTER(C.c_double))
+        c.charge = charge.ctypes.data_as(C.POINTER(C.c_double))
+        c.tip_pair = C.cast(pairs, C.POINTER(_abi.Pair))
+        return Desc(c, keep=(self, pos, charge, pairs))
+
+    def pair_params(self) -> np.ndarray:
+        return np.array([[self.c.tip_pair[t].p[m] for m in range(3)]
+                         for t in range(self.c.n_types)]).reshape(self.c.n_types, 3)
+
+    def pair_kinds(self) -> np.ndarray:
+        return np.array([self.c.tip_pair[t].kind for t in range(self.c.n_types)], dtype=np.int32)
+
     @property
     def n_columns(self) -> int:
         return self.c.nx * self.c.ny
@@ -135,6 +161,24 @@ class Scan:
         check(lib().mafm_run(self._h, C.byref(o), C.c_void_p(out_ptr),
                              C.byref(st) if st is not None else None, stream))
         return st
+
+    def adjoint(self, points: np.ndarray, dl_dfz: np.ndarray, stream=None) -> dict:
+        """Gradients of L through the relaxation, given the relaxed points of a
+        run and dL/dFz per point (mafm_adjoint): dpos (n_atoms, 3), dcharge
+        (n_atoms,), dpair (n_types, 3) for tip_pair[t].p."""
+        d = self.desc.c
+        points = np.ascontiguousarray(points, dtype=_abi.POINT_DTYPE)
+        w = np.ascontiguousarray(dl_dfz, dtype=np.float64).reshape(-1)
+        if len(points) != self.desc.n_points or len(w) != self.desc.n_points:
+            raise ValueError("adjoint needs every point of the scan")
+        dpos = np.zeros((d.n_atoms, 3))
+        dq = np.zeros(d.n_atoms)
+        dpair = np.zeros((d.n_types, 3))
+        g = _abi.Grad(dpos.ctypes.data_as(C.POINTER(C.c_double)),
+                      dq.ctypes.data_as(C.POINTER(C.c_double)),
+                      dpair.ctypes.data_as(C.POINTER(C.c_double)))
+        check(lib().mafm_adjoint(self._h, ptr(points), ptr(w), C.byref(g), stream))
+        return {"dpos": dpos, "dcharge": dq, "dpair": dpair}
 
     def sample(self, pts: np.ndarray, precision=_abi.FP64, what: int = 0) -> np.ndarray:
         pts = np.ascontiguousarray(pts, dtype=np.float64).reshape(-1, 3)

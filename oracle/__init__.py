@@ -47,6 +47,9 @@ def port():
         L.oracle_grid.restype = C.c_int
         L.oracle_grid.argtypes = [C.POINTER(_abi.ScanDesc), C.c_int, C.c_int32 * 3,
                                   C.c_void_p, C.c_int64]
+        L.oracle_adjoint.restype = C.c_int
+        L.oracle_adjoint.argtypes = [C.POINTER(_abi.ScanDesc), C.c_void_p, C.c_void_p, C.c_void_p,
+                                     C.c_void_p, C.c_void_p]
         L.oracle_last_error.restype = C.c_char_p
         _port = L
     return _port
@@ -77,6 +80,19 @@ def sample(desc, pts: np.ndarray, what: int = 0) -> np.ndarray:
     _check(port().oracle_sample(C.byref(desc.c), what, pts.ctypes.data_as(C.c_void_p),
                                 len(pts), out.ctypes.data_as(C.c_void_p)))
     return out
+
+
+def adjoint(desc, pts, w):
+    """FP64 gradients of sum_p w_p Fz_p (see oracle_adjoint): dpos, dcharge, dpair."""
+    d = desc.c
+    dpos = np.zeros((d.n_atoms, 3))
+    dq = np.zeros(d.n_atoms)
+    dpair = np.zeros((d.n_types, 3))
+    w = np.ascontiguousarray(w, dtype=np.float64)
+    _check(port().oracle_adjoint(C.byref(d), pts.ctypes.data_as(C.c_void_p),
+                                 w.ctypes.data_as(C.c_void_p), dpos.ctypes.data_as(C.c_void_p),
+                                 dq.ctypes.data_as(C.c_void_p), dpair.ctypes.data_as(C.c_void_p)))
+    return {"dpos": dpos, "dcharge": dq, "dpair": dpair}
 
 
 def grid(desc, what: int = 0) -> np.ndarray:

@@ -713,3 +713,175 @@ int oracle_grid(const mafm_scan_desc* d, int what, int32_t n[3], double* out, in
     ctx_free(&c);
     return 0;
 }
+
+/* ---- adjoint (implicit differentiation at the relaxed points) ------------
+ * Same formulas as the product's adjoint kernel, written plainly: per point,
+ * J = dF_total/dx, lambda = J^-T (row z of dF_ts/dx), mu = w (e_z - lambda),
+ * and every term contributes mu . df/dtheta.  The reference itself has no
+ * derivatives; this restatement is checked against central finite differences
+ * of the oracle's own relaxation in tests/test_adjoint.py. */
+static void pair_s_o(int kind, double p0, double p1, double p2, double r2, double* s, double* dsr) {
+    if (kind == MAFM_PAIR_LJ) {
+        double ir2 = 1.0 / r2, ir6 = ir2 * ir2 * ir2;
+        double a12 = p1 * ir6 * ir6, a6 = p0 * ir6;
+        *s = (12 * a12 - 6 * a6) * ir2;
+        *dsr = (-168 * a12 + 48 * a6) * ir2 * ir2;
+    } else {
+        double r = sqrt(r2), d = exp(-p1 * (r - p2));
+        double g = 2 * p0 * p1 * (d * d - d), dg = 2 * p0 * p1 * (2 * d - 1) * (-p1 * d);
+        *s = g / r;
+        *dsr = (dg / r - g / r2) / r;
+    }
+}
+
+static void pair_dparam_o(int kind, double p0, double p1, double p2, double r2, double q[3]) {
+    if (kind == MAFM_PAIR_LJ) {
+        double ir2 = 1.0 / r2, ir6 = ir2 * ir2 * ir2;
+        q[0] = -6 * ir6 * ir2;
+        q[1] = 12 * ir6 * ir6 * ir2;
+        q[2] = 0;
+    } else {
+        double r = sqrt(r2), x = r - p2, d = exp(-p1 * x), dd = d * d - d;
+        q[0] = 2 * p1 * dd / r;
+        q[1] = (2 * p0 * dd + 2 * p0 * p1 * (2 * d - 1) * (-x * d)) / r;
+        q[2] = 2 * p0 * p1 * (2 * d - 1) * (p1 * d) / r;
+    }
+}
+
+static void es_jac_o(const Grid* g, v3 pos, double Jg[9]) {
+    double q[3] = {pos.x - g->origin[0], pos.y - g->origin[1], pos.z - g->origin[2]}, pb[3], d[3];
+    int gp[3];
+    for (int a = 0; a < 3; ++a) {
+        pb[a] = g->inv[a][0] * q[0] + g->inv[a][1] * q[1] + g->inv[a][2] * q[2];
+        gp[a] = (int)floor(pb[a]);
+        d[a] = pb[a] - gp[a];
+    }
+    double dFd[3][3] = {{0}};
+    for (int c = 0; c < 8; ++c) {
+        int idx[3] = {gp[0] + (c >> 2), gp[1] + ((c >> 1) & 1), gp[2] + (c & 1)};
+        for (int a = 0; a < 3; ++a) {
+            idx[a] %= g->n[a];
+            if (idx[a] < 0) idx[a] += g->n[a];
+        }
+        const double* v = g->fe + 4 * (((size_t)idx[0] * g->n[1] + idx[1]) * g->n[2] + idx[2]);
+        double w[3] = {(c >> 2) ? d[0] : 1 - d[0], ((c >> 1) & 1) ? d[1] : 1 - d[1], (c & 1) ? d[2] : 1 - d[2]};
+        double sg[3] = {(c >> 2) ? 1.0 : -1.0, ((c >> 1) & 1) ? 1.0 : -1.0, (c & 1) ? 1.0 : -1.0};
+        double dw[3] = {sg[0] * w[1] * w[2], sg[1] * w[0] * w[2], sg[2] * w[0] * w[1]};
+        for (int m = 0; m < 3; ++m)
+            for (int a = 0; a < 3; ++a) dFd[m][a] += v[m] * dw[a];
+    }
+    for (int m = 0; m < 3; ++m)
+        for (int j = 0; j < 3; ++j)
+            Jg[3 * m + j] = dFd[m][0] * g->inv[0][j] + dFd[m][1] * g->inv[1][j] + dFd[m][2] * g->inv[2][j];
+}
+
+int oracle_adjoint(const mafm_scan_desc* d, const mafm_point* pts, const double* w, double* dpos,
+                   double* dcharge, double* dpair) {
+    Ctx c;
+    int st = ctx_init(&c, d);
+    if (st) { ctx_free(&c); return st; }
+    if (c.mode == 2) { ctx_free(&c); return MAFM_E_UNSUPPORTED; }
+    const int na = d->n_atoms;
+    memset(dpos, 0, sizeof(double) * 3 * na);
+    memset(dcharge, 0, sizeof(double) * na);
+    memset(dpair, 0, sizeof(double) * 3 * d->n_types);
+    const double qbq = d->qbase * d->tip_charge;
+    const long long npts = (long long)d->nx * d->ny * d->nz;
+    for (long long p = 0; p < npts; ++p) {
+        const long long col = p / d->nz;
+        const int k = (int)(p % d->nz);
+        double dx, dy;
+        dummy_xy(&c, d->tip_pbc && !d->rigidgrid, (int)(col / d->ny) * d->dx, (int)(col % d->ny) * d->dy, &dx, &dy);
+        double dz = d->zhigh;
+        for (int s = 0; s < k; ++s) dz -= d->dz;
+        v3 x = {pts[p].tip[0], pts[p].tip[1], pts[p].tip[2]};
+        double J[9] = {0};
+        for (int t = 0; t < c.nt; ++t) {
+            const Term* tm = &c.terms[t];
+            v3 r = {x.x - tm->x, x.y - tm->y, x.z - tm->z};
+            double r2 = r.x * r.x + r.y * r.y + r.z * r.z, s, dsr;
+            pair_s_o(tm->kind, tm->p0, tm->p1, tm->p2, r2, &s, &dsr);
+            if (tm->coul) {
+                double ir = 1.0 / sqrt(r2), ir3 = ir * ir * ir;
+                s += tm->qq * ir3;
+                dsr += -3 * tm->qq * ir3 * ir * ir;
+            }
+            double rv[3] = {r.x, r.y, r.z};
+            for (int a = 0; a < 3; ++a)
+                for (int b = 0; b < 3; ++b) J[3 * a + b] += (a == b ? s : 0) + dsr * rv[a] * rv[b];
+        }
+        if (c.mode == 1) {
+            double Jg[9];
+            es_jac_o(&c.es, x, Jg);
+            for (int m = 0; m < 9; ++m) J[m] += Jg[m];
+        }
+        double cz[3] = {J[6], J[7], J[8]};
+        {
+            v3 r = {x.x - dx, x.y - dy, x.z - dz};
+            double r2 = r.x * r.x + r.y * r.y + r.z * r.z, s, dsr;
+            pair_s_o(d->dummy_pair.kind, d->dummy_pair.p[0], d->dummy_pair.p[1], d->dummy_pair.p[2], r2, &s, &dsr);
+            if (d->tip_dummy_coulomb && d->dummy_charge != 0 && d->tip_charge != 0) {
+                double qq = d->qbase * d->dummy_charge * d->tip_charge;
+                double ir = 1.0 / sqrt(r2), ir3 = ir * ir * ir;
+                s += qq * ir3;
+                dsr += -3 * qq * ir3 * ir * ir;
+            }
+            double rv[3] = {r.x, r.y, r.z};
+            for (int a = 0; a < 3; ++a)
+                for (int b = 0; b < 3; ++b) J[3 * a + b] += (a == b ? s : 0) + dsr * rv[a] * rv[b];
+            double rho = sqrt(r.x * r.x + r.y * r.y), k2 = 2 * d->harm_k;
+            if (d->harm_r0 == 0.0 || rho <= 1e-10) {
+                J[0] -= k2;
+                J[4] -= k2;
+            } else {
+                double f = 1 - d->harm_r0 / rho, g = d->harm_r0 / (rho * rho * rho);
+                J[0] -= k2 * (f + g * r.x * r.x);
+                J[4] -= k2 * (f + g * r.y * r.y);
+                J[1] -= k2 * g * r.x * r.y;
+                J[3] -= k2 * g * r.x * r.y;
+            }
+        }
+        /* lambda = J^-T cz by Gaussian elimination on J^T */
+        double A[3][4];
+        for (int a = 0; a < 3; ++a) {
+            for (int b = 0; b < 3; ++b) A[a][b] = J[3 * b + a];
+            A[a][3] = cz[a];
+        }
+        for (int col2 = 0; col2 < 3; ++col2) {
+            int piv = col2;
+            for (int r2 = col2 + 1; r2 < 3; ++r2)
+                if (fabs(A[r2][col2]) > fabs(A[piv][col2])) piv = r2;
+            for (int m = 0; m < 4; ++m) { double tmp = A[col2][m]; A[col2][m] = A[piv][m]; A[piv][m] = tmp; }
+            for (int r2 = 0; r2 < 3; ++r2) {
+                if (r2 == col2) continue;
+                double f = A[r2][col2] / A[col2][col2];
+                for (int m = col2; m < 4; ++m) A[r2][m] -= f * A[col2][m];
+            }
+        }
+        double lam[3] = {A[0][3] / A[0][0], A[1][3] / A[1][1], A[2][3] / A[2][2]};
+        double mu[3] = {-w[p] * lam[0], -w[p] * lam[1], w[p] * (1 - lam[2])};
+        for (int t = 0; t < c.nt; ++t) {
+            const Term* tm = &c.terms[t];
+            const int a = t % na;
+            v3 r = {x.x - tm->x, x.y - tm->y, x.z - tm->z};
+            double r2 = r.x * r.x + r.y * r.y + r.z * r.z, s, dsr, ir3 = 0;
+            pair_s_o(tm->kind, tm->p0, tm->p1, tm->p2, r2, &s, &dsr);
+            if (tm->coul) {
+                double ir = 1.0 / sqrt(r2);
+                ir3 = ir * ir * ir;
+                s += tm->qq * ir3;
+                dsr += -3 * tm->qq * ir3 * ir * ir;
+            }
+            double rm = r.x * mu[0] + r.y * mu[1] + r.z * mu[2];
+            dpos[3 * a] -= s * mu[0] + dsr * r.x * rm;
+            dpos[3 * a + 1] -= s * mu[1] + dsr * r.y * rm;
+            dpos[3 * a + 2] -= s * mu[2] + dsr * r.z * rm;
+            double q[3];
+            pair_dparam_o(tm->kind, tm->p0, tm->p1, tm->p2, r2, q);
+            for (int m = 0; m < 3; ++m) dpair[3 * d->type[a] + m] += q[m] * rm;
+            if (tm->coul) dcharge[a] += qbq * ir3 * rm;
+        }
+    }
+    ctx_free(&c);
+    return 0;
+}

@@ -1,0 +1,178 @@
+"""Gradients through the relaxation (mafm_adjoint), checked three ways:
+  * the oracle's FP64 adjoint (oracle_adjoint) against central finite
+    differences of the oracle's own relaxation (CPU);
+  * the GPU adjoint against the oracle adjoint on the same relaxed points (GPU);
+  * the GPU adjoint against central differences of the GPU's FP64 relaxation,
+    and the torch.autograd wrapper against the oracle (GPU).
+
+Finite differences: h = 1e-4 (absolute for positions and charges, relative for
+pair parameters), with the relaxation converged to |F| < 1e-10 so that the
+difference quotient measures the derivative and not the stopping tolerance.
+Tolerance: 1e-4 relative to max(|g_fd|, 1e-3 * max|g|) (the adjoint bar).
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import oracle
+from mechafm_gb300 import _abi, synth
+from mechafm_gb300.scan import Input, Scan
+
+REL = 1e-4
+
+
+def tight_cluster(tmp, **opt):
+    spec = synth.cluster_60(area=0.3, step=0.1, zhigh=10.0, zlow=9.7, minterm="f",
+                            ftol="1e-10", maxsteps="400000", **opt)
+    return Input(spec.write(str(tmp))).desc()
+
+
+class Perturb:
+    """Own copies of the perturbable descriptor arrays."""
+
+    def __init__(self, desc):
+        d = desc.c
+        self.desc = desc
+        self.pos = np.ctypeslib.as_array(d.pos, shape=(d.n_atoms * 3,)).copy()
+        self.chg = np.ctypeslib.as_array(d.charge, shape=(d.n_atoms,)).copy()
+        self.pairs = (_abi.Pair * d.n_types)(*[d.tip_pair[t] for t in range(d.n_types)])
+        d.pos = self.pos.ctypes.data_as(C.POINTER(C.c_double))
+        d.charge = self.chg.ctypes.data_as(C.POINTER(C.c_double))
+        d.tip_pair = C.cast(self.pairs, C.POINTER(_abi.Pair))
+
+    def cases(self):
+        """(name, getter/setter, step) for a spread of parameters."""
+        out = []
+        for a in (3, 17, 40):
+            for k in range(3):
+                out.append((f"pos{a}.{k}", self._arr(self.pos, 3 * a + k), 1e-4))
+        for t in range(self.desc.c.n_types):
+            for m in range(3):
+                v = self.pairs[t].p[m]
+                if v != 0:
+                    out.append((f"pair{t}.{m}", self._pair(t, m), 1e-4 * abs(v)))
+        for a in (5, 22):
+            out.append((f"q{a}", self._arr(self.chg, a), 1e-4))
+        return out
+
+    @staticmethod
+    def _arr(arr, i):
+        def gs(v=None):
+            if v is None:
+                return arr[i]
+            arr[i] = v
+        return gs
+
+    def _pair(self, t, m):
+        def gs(v=None):
+            if v is None:
+                return self.pairs[t].p[m]
+            self.pairs[t].p[m] = v
+        return gs
+
+
+def grad_of(g, name):
+    if name.startswith("pos"):
+        a, k = map(int, name[3:].split("."))
+        return g["dpos"][a, k]
+    if name.startswith("pair"):
+        t, m = map(int, name[4:].split("."))
+        return g["dpair"][t, m]
+    return g["dcharge"][int(name[1:])]
+
+
+def fd_check(g, pert, loss):
+    scale = 1e-3 * max(np.abs(g["dpos"]).max(), np.abs(g["dcharge"]).max())
+    for name, gs, h in pert.cases():
+        v0 = gs()
+        gs(v0 + h)
+        lp = loss()
+        gs(v0 - h)
+        lm = loss()
+        gs(v0)
+        fd = (lp - lm) / (2 * h)
+        ad = grad_of(g, name)
+        assert abs(ad - fd) <= REL * max(abs(fd), scale * (abs(h) if name.startswith("pair") else 1)) \
+            or abs(ad - fd) <= 1e-9, (name, ad, fd)
+
+
+def test_oracle_adjoint_matches_finite_differences(tmp_path):
+    desc = tight_cluster(tmp_path)
+    pert = Perturb(desc)
+    pts, _ = oracle.run(desc)
+    assert (pts["steps"] < 400000).all()
+    w = np.random.default_rng(3).normal(size=len(pts))
+    g = oracle.adjoint(desc, pts, w)
+
+    def loss():
+        p, _ = oracle.run(desc)
+        return float((w * p["force"][:, 2]).sum())
+
+    fd_check(g, pert, loss)
+
+
+@pytest.mark.gpu
+def test_gpu_adjoint_matches_oracle_adjoint(tmp_path):
+    desc = tight_cluster(tmp_path)
+    scan = Scan(desc, device=0)
+    pts, _ = scan.run(_abi.FP64)
+    w = np.random.default_rng(4).normal(size=len(pts))
+    g = scan.adjoint(pts, w)
+    want = oracle.adjoint(desc, pts, w)
+    for key in ("dpos", "dcharge", "dpair"):
+        scale = np.abs(want[key]).max()
+        np.testing.assert_allclose(g[key], want[key], rtol=1e-9, atol=1e-12 * max(scale, 1.0))
+
+
+@pytest.mark.gpu
+def test_gpu_adjoint_matches_gpu_finite_differences(tmp_path):
+    desc = tight_cluster(tmp_path)
+    pert = Perturb(desc)
+    scan = Scan(desc, device=0)
+    pts, _ = scan.run(_abi.FP64)
+    w = np.random.default_rng(5).normal(size=len(pts))
+    g = scan.adjoint(pts, w)
+
+    def loss():
+        s = Scan(desc, device=0)
+        p, _ = s.run(_abi.FP64)
+        s.close()
+        return float((w * p["force"][:, 2]).sum())
+
+    fd_check(g, pert, loss)
+
+
+@pytest.mark.gpu
+def test_external_field_adjoint_matches_oracle():
+    from conftest import golden
+    desc = Input(golden("slab_es").input).desc()
+    scan = Scan(desc, device=0)
+    pts, _ = scan.run(_abi.FP64)
+    w = np.random.default_rng(6).normal(size=len(pts))
+    g = scan.adjoint(pts, w)
+    want = oracle.adjoint(desc, pts, w)
+    for key in ("dpos", "dpair"):
+        scale = np.abs(want[key]).max()
+        np.testing.assert_allclose(g[key], want[key], rtol=1e-7, atol=1e-9 * max(scale, 1.0))
+
+
+@pytest.mark.gpu
+def test_torch_autograd_matches_oracle(tmp_path):
+    torch = pytest.importorskip("torch")
+    from mechafm_gb300.torch_ops import fz_image
+    desc = tight_cluster(tmp_path)
+    a = desc.atoms()
+    pos = torch.tensor(a["pos"], requires_grad=True)
+    chg = torch.tensor(a["charge"], requires_grad=True)
+    pair = torch.tensor(desc.pair_params(), requires_grad=True)
+    fz = fz_image(desc, pos, chg, pair)
+    target = fz.detach() + 0.01 * torch.randn_like(fz)
+    loss = ((fz - target) ** 2).mean()
+    loss.backward()
+    pts, _ = oracle.run(desc)
+    w = (2 * (pts["force"][:, 2] - target.numpy().reshape(-1)) / fz.numel())
+    want = oracle.adjoint(desc, pts, w)
+    np.testing.assert_allclose(pos.grad.numpy(), want["dpos"], rtol=1e-8, atol=1e-12)
+    np.testing.assert_allclose(chg.grad.numpy(), want["dcharge"], rtol=1e-8, atol=1e-12)
+    np.testing.assert_allclose(pair.grad.numpy(), want["dpair"], rtol=1e-8, atol=1e-20)
