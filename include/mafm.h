@@ -274,6 +274,29 @@ typedef struct mafm_grad {
 int mafm_adjoint(mafm_scan* scan, const mafm_point* pts, const double* dl_dfz, mafm_grad* out,
                  void* stream);
 
+/* ---- frequency-shift images ------------------------------------------------
+ * The reference's post-processing (simple-vafm-image.py:77-89, 204) turns Fz
+ * stacks into frequency-shift images with Giessibl's weights; these run that
+ * operator on the GPU.  Parameters default (params = NULL) to the script's
+ * A = 0.5 A, k = 1800 N/m = 1800*1.438978 kcal/mol/A^2, f0 = 25 kHz. */
+typedef struct mafm_df_params {
+    double amplitude;       /* oscillation amplitude A (Angstrom) */
+    double k_cantilever;    /* cantilever stiffness (energy unit / A^2) */
+    double f0;              /* resonance frequency (Hz) */
+} mafm_df_params;
+/* The window weights W (n_w values) and fshiftfac for height step dz. */
+int mafm_df_weights(const mafm_df_params* params, double dz, double* w, int32_t cap, int32_t* n_w,
+                    double* fshiftfac);
+/* df[s][x][y] for every window s of n_w heights (nz - n_w windows, ascending
+ * z): fz[((x*ny + y)*nz + k) * stride] is Fz at scan level k (k = 0 at zhigh);
+ * stride 8 reads mafm_point.force[2] (pass &pts[0].force[2]).  Host or device
+ * memory. */
+int mafm_df(const double* fz, int64_t stride, int32_t nx, int32_t ny, int32_t nz, double dz,
+            const mafm_df_params* params, double* df, void* stream);
+/* Transpose of mafm_df: dL/dFz (nx*ny*nz, level order) from dL/ddf. */
+int mafm_df_adjoint(const double* g_df, int32_t nx, int32_t ny, int32_t nz, double dz,
+                    const mafm_df_params* params, double* g_fz, void* stream);
+
 /* Evaluate the tip–surface force and energy at n given tip positions
  * (System::evalTipSurfaceForces, system.cpp:41-51): pairs, external field or
  * rigid grid, whatever the scan uses.  what: 0 = all tip–surface terms,

@@ -77,6 +77,10 @@ class RunStats(C.Structure):
                 ("reserved", C.c_uint32), ("kernel_ms", C.c_double)]
 
 
+class DfParams(C.Structure):
+    _fields_ = [("amplitude", C.c_double), ("k_cantilever", C.c_double), ("f0", C.c_double)]
+
+
 class Grad(C.Structure):
     _fields_ = [("dpos", C.POINTER(C.c_double)), ("dcharge", C.POINTER(C.c_double)),
                 ("dpair", C.POINTER(C.c_double))]
@@ -109,6 +113,12 @@ SIGNATURES = {
     "mafm_autotune": (C.c_int, [C.POINTER(_P), C.c_int32, C.POINTER(RunOpts),
                                 C.POINTER(C.c_double), _P]),
     "mafm_adjoint": (C.c_int, [_P, _P, _P, C.POINTER(Grad), _P]),
+    "mafm_df_weights": (C.c_int, [C.POINTER(DfParams), C.c_double, _P, C.c_int32,
+                                  C.POINTER(C.c_int32), C.POINTER(C.c_double)]),
+    "mafm_df": (C.c_int, [_P, C.c_int64, C.c_int32, C.c_int32, C.c_int32, C.c_double,
+                          C.POINTER(DfParams), _P, _P]),
+    "mafm_df_adjoint": (C.c_int, [_P, C.c_int32, C.c_int32, C.c_int32, C.c_double,
+                                  C.POINTER(DfParams), _P, _P]),
     "mafm_scan_sample": (C.c_int, [_P, C.c_int32, C.c_int32, _P, C.c_int64, _P]),
     "mafm_scan_grid_info": (C.c_int, [_P, C.c_int32, C.c_int32 * 3, C.c_double * 9,
                                       C.c_double * 3]),
