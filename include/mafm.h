@@ -311,6 +311,14 @@ int mafm_scan_grid_info(const mafm_scan* scan, int32_t what, int32_t n[3],
                         double basis[9], double origin[3]);
 /* Copy the FP64 grid nodes {Fx,Fy,Fz,E} (n0*n1*n2*4 doubles, z fastest). */
 int mafm_scan_grid_copy(const mafm_scan* scan, int32_t what, double* out);
+/* (Re)build the rigid force grid of a rigidgrid scan for one precision on the
+ * stream: Simulation::buildTipGridInteractions (simulation.cpp:420-501), which
+ * the reference runs once per scan before the pixel loop.  mafm_run builds the
+ * grid on first use; this call rebuilds it on demand.  The first call for a
+ * precision allocates the grid; later calls only launch the build kernel, so
+ * they may be captured in a CUDA graph together with mafm_plan_launch.
+ * No-op (MAFM_OK) for a scan without a rigid grid. */
+int mafm_scan_build_grid(mafm_scan* scan, int32_t precision, void* stream);
 
 /* ---- output (host) ---------------------------------------------------------
  * Writes scan-%06.3f.dat[.gz] files and statistics.txt exactly as the

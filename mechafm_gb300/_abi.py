@@ -123,6 +123,7 @@ SIGNATURES = {
     "mafm_scan_grid_info": (C.c_int, [_P, C.c_int32, C.c_int32 * 3, C.c_double * 9,
                                       C.c_double * 3]),
     "mafm_scan_grid_copy": (C.c_int, [_P, C.c_int32, _P]),
+    "mafm_scan_build_grid": (C.c_int, [_P, C.c_int32, _P]),
     "mafm_write_output": (C.c_int, [_P, _P, C.c_char_p, C.c_int32]),
     "mafm_write_statistics": (C.c_int, [_P, C.c_char_p, C.c_uint64, C.c_double, C.c_double]),
 }

@@ -481,18 +481,22 @@ void zero_counters(mafm_scan& s, cudaStream_t st) {
     cuda_check(cudaMemsetAsync(s.ctr.p, 0, sizeof(RunCounters), st), "reset counters");
 }
 
-void ensure_grid(mafm_scan& s, bool fp64, cudaStream_t st) {
+void ensure_grid(mafm_scan& s, bool fp64, cudaStream_t st, bool rebuild = false) {
     if (!s.d.rigidgrid) return;
     const long long N = (long long)s.grid_view.n[0] * s.grid_view.n[1] * s.grid_view.n[2];
+    if (rebuild) {
+        if (fp64) s.grid64_built = false;
+        else s.grid32_built = false;
+    }
     if (fp64 && !s.grid64_built) {
-        s.grid64.alloc((size_t)N);
+        if (!s.grid64.p) s.grid64.alloc((size_t)N);
         zero_counters(s, st);
         cuda_check(launch_grid_build64(build_grid_params(s), s.grid_view, s.grid64.p, s.ctr.p, st), "grid build");
         s.grid_view.g64 = s.grid64.p;
         s.grid64_built = true;
     }
     if (!fp64 && !s.grid32_built) {
-        s.grid32.alloc((size_t)N);
+        if (!s.grid32.p) s.grid32.alloc((size_t)N);
         zero_counters(s, st);
         cuda_check(launch_grid_build32(build_grid_params(s), s.grid_view, s.grid32.p, s.ctr.p, st), "grid build");
         s.grid_view.g32 = s.grid32.p;
@@ -845,6 +849,16 @@ int mafm_scan_grid_info(const mafm_scan* scan, int32_t what, int32_t n[3], doubl
             if (origin) origin[a] = g.origin[a];
         }
         if (basis) std::memcpy(basis, g.basis, sizeof g.basis);
+    });
+}
+
+int mafm_scan_build_grid(mafm_scan* scan, int32_t precision, void* stream) {
+    return guarded([&] {
+        if (!scan) fail(MAFM_E_INVALID, "null scan");
+        if (precision != MAFM_FP64 && precision != MAFM_FP32C) fail(MAFM_E_INVALID, "unknown precision %d", precision);
+        if (!scan->d.rigidgrid) return;
+        cuda_check(cudaSetDevice(scan->device), "cudaSetDevice");
+        ensure_grid(*scan, precision == MAFM_FP64, (cudaStream_t)stream, true);
     });
 }
 

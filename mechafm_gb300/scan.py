@@ -86,6 +86,34 @@ class Desc:
         c.tip_pair = C.cast(pairs, C.POINTER(_abi.Pair))
         return Desc(c, keep=(self, pos, charge, pairs))
 
+    def crop(self, i0: int, j0: int, ni: int, nj: int) -> "Desc":
+        """The ni x nj pixel block starting at pixel (i0, j0) as a scan of its
+        own: pixel (i, j) of the copy is pixel (i0 + i, j0 + j) of this scan.
+        The surface, the cell offset and the external field's origin move by
+        -(i0 dx, j0 dy), so every tip–surface distance is unchanged, and the
+        rigid grid of the copy lies on the same lattice (its spacing, dx/2 and
+        dy/2, divides the shift).  Used to time and check sub-areas of scans
+        whose full grid is too large for the FP64 and CPU paths."""
+        d = self.c
+        if not (0 <= i0 and 0 <= j0 and ni >= 1 and nj >= 1 and i0 + ni <= d.nx and j0 + nj <= d.ny):
+            raise ValueError("crop outside the pixel grid")
+        c = _abi.ScanDesc()
+        C.pointer(c)[0] = d
+        sx, sy = i0 * d.dx, j0 * d.dy
+        pos = self.atoms()["pos"]
+        pos[:, 0] -= sx
+        pos[:, 1] -= sy
+        pos = np.ascontiguousarray(pos.reshape(-1))
+        c.pos = pos.ctypes.data_as(C.POINTER(C.c_double))
+        c.nx, c.ny = ni, nj
+        c.area[0] = (ni - 1) * d.dx
+        c.area[1] = (nj - 1) * d.dy
+        c.offset[0] = d.offset[0] - sx
+        c.offset[1] = d.offset[1] - sy
+        c.epot_origin[0] = d.epot_origin[0] - sx
+        c.epot_origin[1] = d.epot_origin[1] - sy
+        return Desc(c, keep=(self, pos))
+
     def pair_params(self) -> np.ndarray:
         return np.array([[self.c.tip_pair[t].p[m] for m in range(3)]
                          for t in range(self.c.n_types)]).reshape(self.c.n_types, 3)

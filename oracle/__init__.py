@@ -41,6 +41,9 @@ def port():
         L.oracle_run.restype = C.c_int
         L.oracle_run.argtypes = [C.POINTER(_abi.ScanDesc), C.c_int, C.c_int, C.c_void_p,
                                  C.c_int, C.POINTER(C.c_uint64)]
+        L.oracle_run_split.restype = C.c_int
+        L.oracle_run_split.argtypes = [C.POINTER(_abi.ScanDesc), C.c_int, C.c_int, C.c_void_p,
+                                       C.c_int, C.POINTER(C.c_uint64), C.c_double * 2]
         L.oracle_sample.restype = C.c_int
         L.oracle_sample.argtypes = [C.POINTER(_abi.ScanDesc), C.c_int, C.c_void_p,
                                     C.c_int64, C.c_void_p]
@@ -72,6 +75,20 @@ def run(desc, col_begin: int = 0, col_end: int | None = None, threads: int = 0):
     _check(port().oracle_run(C.byref(d), col_begin, col_end, out.ctypes.data_as(C.c_void_p),
                              threads, C.byref(steps)))
     return out, int(steps.value)
+
+
+def run_split(desc, col_begin: int = 0, col_end: int | None = None, threads: int = 0):
+    """run() plus its wall time split: (points, total_steps, setup_s, relax_s)."""
+    from mechafm_gb300 import _abi
+    d = desc.c
+    if col_end is None:
+        col_end = d.nx * d.ny
+    out = np.zeros((col_end - col_begin) * d.nz, dtype=_abi.POINT_DTYPE)
+    steps = C.c_uint64(0)
+    t = (C.c_double * 2)()
+    _check(port().oracle_run_split(C.byref(d), col_begin, col_end, out.ctypes.data_as(C.c_void_p),
+                                   threads, C.byref(steps), t))
+    return out, int(steps.value), t[0], t[1]
 
 
 def sample(desc, pts: np.ndarray, what: int = 0) -> np.ndarray:

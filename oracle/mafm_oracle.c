@@ -679,6 +679,29 @@ int oracle_run(const mafm_scan_desc* d, int col_begin, int col_end, mafm_point* 
     return 0;
 }
 
+/* oracle_run with its wall time split into the set-up (terms, external field,
+ * rigid grid: ctx_init) and the relaxation: t[0], t[1] in seconds. */
+int oracle_run_split(const mafm_scan_desc* d, int col_begin, int col_end, mafm_point* out,
+                     int nthreads, uint64_t* total_steps, double t[2]) {
+    const double t0 = omp_get_wtime();
+    Ctx c;
+    int st = ctx_init(&c, d);
+    if (st) { ctx_free(&c); return st; }
+    const double t1 = omp_get_wtime();
+    unsigned long long steps = 0;
+#pragma omp parallel for schedule(dynamic, 1) reduction(+ : steps) num_threads(nthreads > 0 ? nthreads : omp_get_max_threads())
+    for (int col = col_begin; col < col_end; ++col) {
+        mafm_point* o = out + (size_t)(col - col_begin) * d->nz;
+        column(&c, col, o);
+        for (int k = 0; k < d->nz; ++k) steps += (unsigned long long)o[k].steps;
+    }
+    if (total_steps) *total_steps = steps;
+    ctx_free(&c);
+    t[0] = t1 - t0;
+    t[1] = omp_get_wtime() - t1;
+    return 0;
+}
+
 /* Tip–surface F,E at tip positions; what 1 = external field only. */
 int oracle_sample(const mafm_scan_desc* d, int what, const double* pts, int64_t n, double* out) {
     Ctx c;

@@ -253,3 +253,37 @@ def test_autotune_returns_a_valid_fast_shape():
                    tile=best.columns_per_tile)
     tip_err = np.abs(pts["tip"] - case.ref["tip"]).max(axis=1)
     assert (tip_err <= TIP_TOL).mean() >= 0.995
+
+
+def test_grid_rebuild_is_identical_and_captures_with_the_plan():
+    """mafm_scan_build_grid rebuilds the rigid grid bit-identically, and a
+    graph of [grid build, plan launch] reproduces mafm_run's points."""
+    import ctypes as C
+    import torch
+    desc = Input(golden("slab_es_grid").input).desc()
+    scan = Scan(desc, device=0)
+    L = _abi.lib()
+    want64, _ = scan.run(_abi.FP64)
+    g64 = scan.grid()
+    _abi.check(L.mafm_scan_build_grid(scan.handle, _abi.FP64, None))
+    np.testing.assert_array_equal(scan.grid(), g64)
+    np.testing.assert_array_equal(scan.run(_abi.FP64)[0]["tip"], want64["tip"])
+    want, _ = scan.run(_abi.FP32C, lanes=2)
+    out = torch.zeros(desc.n_points * 64, dtype=torch.uint8, device="cuda:0")
+    plan = _plan([scan], [out], _abi.RunOpts(_abi.FP32C, 2, 0, 0, 0, 0))
+    stream = torch.cuda.Stream()
+    sp = C.c_void_p(stream.cuda_stream)
+    graph = torch.cuda.CUDAGraph()
+    torch.cuda.synchronize()
+    with torch.cuda.graph(graph, stream=stream):
+        _abi.check(L.mafm_scan_build_grid(scan.handle, _abi.FP32C, sp))
+        _abi.check(L.mafm_plan_launch(plan, sp))
+    graph.replay()
+    torch.cuda.synchronize()
+    got = _points(out)
+    np.testing.assert_array_equal(got["tip"], want["tip"])
+    np.testing.assert_array_equal(got["steps"], want["steps"])
+    L.mafm_plan_destroy(plan)
+    # a scan without a rigid grid: no-op
+    other = Scan(Input(golden("graphene_ef").input).desc(), device=0)
+    _abi.check(L.mafm_scan_build_grid(other.handle, _abi.FP32C, None))
