@@ -63,7 +63,8 @@ WORKLOADS = {
     "cluster_60": "60-atom C/N/O/H cluster, LJ+Morse+Coulomb, 401x401 px x 41 z",
     "graphene_72": "72-C graphene, LJ, 101x101 px x 41 z",
     "molecule_batch": "256 planar molecules (20-400 atoms, LJ+Coulomb), 64^2/128^2/256^2 px x 41 z",
-    "slab_2048": "2048-atom periodic slab, rigid grid + FFT external field, 512x512 px x 41 z",
+    "slab_2048": "2048-atom periodic slab, rigid grid + FFT external field, 512x512 px x 41 z "
+                 "(dummy 18 -> 14 A, top layer at 6 A, tip charge -0.02 e)",
     "adjoint_128": "60-atom C/N/O/H cluster at 128x128 px x 41 z, forward + adjoint of an "
                    "MSE loss on the Fz image",
 }
@@ -106,7 +107,11 @@ def make_inputs(name, tmp, pixels=0):
         px = pixels or 101
         specs = [synth.graphene_72(area=0.1 * (px - 1))]
     elif name == "slab_2048":
-        specs = [synth.slab(pixels=pixels or 512)]
+        # tip 4-8 A above the top layer, tip charge -0.02 e: the lateral
+        # deflection stays inside the rigid grid's 1.5 A margin (the synthetic
+        # Hartree field of random charges is strong; at -0.1 e or 2 A closer
+        # the tip leaves the grid and the reference stops)
+        specs = [synth.slab(pixels=pixels or 512, zhigh=18.0, zlow=14.0, tip_charge=-0.02)]
     else:
         specs = synth.molecule_batch()
     inputs = [Input(s.write(os.path.join(tmp, f"s{i:03d}"))) for i, s in enumerate(specs)]

@@ -258,7 +258,8 @@ def gaussian_potential(pos: np.ndarray, q: np.ndarray, cell: np.ndarray, n: tupl
 def slab(seed: int = 7, nlx: int = 16, nly: int = 32, layers: int = 4,
          cell=(40.0, 40.0, 30.0), cube_n=(160, 160, 120), pixels: int = 512,
          step: float = 0.2, zhigh: float = 16.0, zlow: float = 12.0, dz: float = 0.1,
-         rigidgrid: bool = True, external: bool = True, **opt) -> ScanInput:
+         rigidgrid: bool = True, external: bool = True, tip_charge: float = -0.1,
+         **opt) -> ScanInput:
     """Periodic slab (layers of nlx x nly sites), vdw_pbc, optional cube and grid."""
     rng = np.random.default_rng(seed)
     a, b, c = cell
@@ -273,7 +274,7 @@ def slab(seed: int = 7, nlx: int = 16, nly: int = 32, layers: int = 4,
     pos = np.array(pos)
     q = rng.normal(0.0, 0.3, size=len(pos))
     params = {"C": (0.086, 3.4, 12.011, 0.0), "N": (0.17, 3.25, 14.007, 0.0),
-              TIP[0]: (TIP[1], TIP[2], 15.999, -0.1), DUMMY[0]: (DUMMY[1], DUMMY[2], 0.0, 0.0)}
+              TIP[0]: (TIP[1], TIP[2], 15.999, tip_charge), DUMMY[0]: (DUMMY[1], DUMMY[2], 0.0, 0.0)}
     area = step * (pixels - 1)
     o = base_options(area=f"{area!r} {area!r}", dx=step, dy=step, zhigh=zhigh, zlow=zlow,
                      dz=dz, vdw_pbc="on", rigidgrid="on" if rigidgrid else "off")

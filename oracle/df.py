@@ -42,3 +42,14 @@ def df_images(fz_levels, dz, **prm):
         FZ = asc[:, :, pl:pl + nosc]
         out[pl] = -fac * (FZ * w).sum(axis=2) * dz
     return out
+
+
+def df_adjoint(g_df, nz, dz, **prm):
+    """Transpose of df_images: g_df (nshift, nx, ny) -> dL/dFz (nx, ny, nz), level order."""
+    w, fac = weights(dz, **prm)
+    nosc = len(w)
+    nshift, nx, ny = g_df.shape
+    asc = np.zeros((nx, ny, nz))
+    for pl in range(nshift):
+        asc[:, :, pl:pl + nosc] += (-fac * dz) * g_df[pl][:, :, None] * w
+    return asc[:, :, ::-1]

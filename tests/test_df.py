@@ -93,3 +93,37 @@ def test_df_torch_device_and_grad():
     img.backward(g)
     np.testing.assert_allclose(fz.grad.cpu().numpy(),
                                df.df_adjoint(g.cpu().numpy(), 25, dz), rtol=0, atol=1e-15)
+
+
+def test_oracle_df_adjoint_is_transpose():
+    dz, nz = 0.1, 21
+    x = _stack(7, nz=nz)
+    y = np.random.default_rng(8).normal(size=(nz - len(odf.weights(dz)[0]), 7, 5))
+    lhs = float((odf.df_images(x, dz) * y).sum())
+    rhs = float((x * odf.df_adjoint(y, nz, dz)).sum())
+    assert abs(lhs - rhs) <= 1e-12 * max(abs(lhs), 1.0)
+
+
+@pytest.mark.gpu
+def test_df_loss_backpropagates_through_the_relaxation(tmp_path):
+    """fz_image -> df_image_torch -> loss: the atom-position gradient equals the
+    oracle adjoint driven by the transposed df operator."""
+    torch = pytest.importorskip("torch")
+    import oracle
+    from mechafm_gb300 import synth
+    from mechafm_gb300.scan import Input
+    from mechafm_gb300.torch_ops import fz_image
+    spec = synth.cluster_60(area=0.3, step=0.1, zhigh=10.0, zlow=8.5, minterm="f",
+                            ftol="1e-10", maxsteps="400000")
+    desc = Input(spec.write(str(tmp_path))).desc()
+    dz = desc.c.dz
+    a = desc.atoms()
+    pos = torch.tensor(a["pos"], requires_grad=True)
+    fz = fz_image(desc, pos, torch.tensor(a["charge"]), torch.tensor(desc.pair_params()))
+    img = df.df_image_torch(fz.cuda(), dz)
+    g = torch.randn_like(img)
+    (img * g).sum().backward()
+    pts, _ = oracle.run(desc)
+    w = odf.df_adjoint(g.cpu().numpy(), desc.c.nz, dz).reshape(-1)
+    want = oracle.adjoint(desc, pts, w)["dpos"]
+    np.testing.assert_allclose(pos.grad.numpy(), want, rtol=1e-6, atol=1e-9 * np.abs(want).max())
