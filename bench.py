@@ -54,6 +54,11 @@ L2_FLUSH_BYTES = 512 << 20
 FLOPS_LJ, FLOPS_MORSE, FLOPS_COUL = 25, 29, 20
 # Algorithmic bytes of one trilinear lookup: 8 FP32 {F, E} nodes.
 BYTES_LOOKUP = 8 * 16
+# DRAM bytes (read + write) per relaxed point of relax32_kernel, from one ncu
+# capture of the cluster at 285 x 285 px x 41 z (173.2 MB for 3,330,225
+# points); the traffic is the 64 B output record per point, so it scales with
+# the points.
+DRAM_BYTES_PER_POINT = 173.2e6 / 3330225
 CPU_TARGET_S = 10.0        # CPU sample length
 RIGID_CROP = 16            # pixels per side of the rigid-grid CPU sample
 FP64_RIGID_CROP = 64       # pixels per side of the rigid-grid FP64 comparison
@@ -418,6 +423,24 @@ def time_events(stream, fn, reps=1):
     return float(np.mean(ts))
 
 
+def job_ms(times, world, device):
+    """Mean step time of this rank, then the maximum over ranks (every rank
+    relaxes its own replica; the job ends with the slowest)."""
+    import torch
+    ms = float(np.mean(times))
+    if world > 1:
+        torch.distributed.barrier()
+        t = torch.tensor([ms], dtype=torch.float64, device=device)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    return ms
+
+
+def replica_throughput(points_per_rank, world, ms):
+    """Whole-job points/s: every rank relaxes points_per_rank in ms."""
+    return world * points_per_rank / (ms / 1000.0)
+
+
 def fp32_roofline(achieved, peak, extra):
     r = {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
          "frac": achieved / peak, "traffic": None,
@@ -555,14 +578,8 @@ def ours(args, rank, world, local):
                 e1.record(stream)
             torch.cuda.synchronize()
             times.append(e0.elapsed_time(e1))
-    if world > 1:
-        torch.distributed.barrier()
-    ms = float(np.mean(times))
-    if world > 1:
-        t = torch.tensor([ms], device=f"cuda:{dev}")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-    value = world * n_pts / (ms / 1000.0)
+    ms = job_ms(times, world, f"cuda:{dev}")
+    value = replica_throughput(n_pts, world, ms)
     _abi.check(L.mafm_plan_stats(plan, C.byref(st), sptr))   # the last replay ended cleanly
 
     # the kernels apart, for the rooflines
@@ -639,6 +656,10 @@ def ours(args, rank, world, local):
         relax_line = None
         if fpe.any():
             relax_line = fp32_roofline(relax_flops / (ms_relax / 1000.0) / 1e12, peak_tflops, {
+                "traffic": DRAM_BYTES_PER_POINT * n_pts,
+                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one "
+                                  "285x285x41 cluster launch, scaled by points (the output "
+                                  "records are the traffic)",
                 "kernel": "relax32_kernel", "kernel_ms": ms_relax,
                 "flops_per_force_eval": float((wts * fpe).sum() / wts.sum()),
                 "force_evals": int(st.force_evals)})

@@ -7,6 +7,9 @@
 //                           atoms the inner loop; positions already carry the
 //                           image shift (interactions.cpp:16,30).
 //   atoms32  AtomRec32[n]   32 B per term: float4 {x,y,z,qq} + float4 {p0,p1,p2,kind}
+//   units32  TermPair32[u]  the FP32 terms two by two for packed (f32x2)
+//                           arithmetic: the LJ terms, then the Morse terms,
+//                           each run padded to an even count with a zero term
 //   grid64   Node64[n]     rigid force grid {Fx,Fy,Fz,E}, index (i*ny+j)*nz+k
 //   grid32   float4[n]      same in FP32
 //   es64/es32               external-field grid, same layout
@@ -76,6 +79,19 @@ struct __align__(16) AtomRec32 {
     float4 b;              // p0, p1, p2, kind (int bits)
 };
 
+// Two FP32 terms side by side (component 0: term 2u, component 1: term 2u+1)
+// for the relax kernel's packed arithmetic.  Signs are stored so that the
+// loop needs packed adds, multiplies and FMAs only: positions, qq and LJ's
+// es6 negated, Morse's a and re negated and its force prefactor stored as
+// -2 De a.  A padding
+// term has zero parameters and sits far away, so every part of it is 0.
+struct __align__(16) TermPair32 {
+    float4 xy;             // -x0, -x1, -y0, -y1
+    float4 zq;             // -z0, -z1, -qq0, -qq1
+    float4 pa;             // LJ -es6_0, -es6_1, es12_0, es12_1 | Morse De_0, De_1, -a_0, -a_1
+    float4 pb;             // Morse -re_0, -re_1, -2 De a_0, -2 De a_1 (zero for LJ)
+};
+
 // A trilinear force grid (ForceGrid, force_grid.hpp:15-51).
 struct GridView {
     const Node64* g64;
@@ -96,6 +112,9 @@ struct ScanParams {
     int n_terms_direct;    // terms evaluated per force call (0 in rigid-grid mode)
     const AtomRec64* atoms64;
     const AtomRec32* atoms32;
+    const TermPair32* units32;
+    int n_units;           // TermPair32 records
+    int n_units_lj;        // of which the first n_units_lj hold LJ terms
     // tip–surface source of the relax: 0 pairs, 1 pairs + external field, 2 rigid grid
     int ts_mode;
     int has_coulomb;       // any term carries a Coulomb part

@@ -148,6 +148,100 @@ __device__ __forceinline__ void pair32(const AtomRec32& t, float dx, float dy, f
     v[3] += e;
 }
 
+// ---- packed (f32x2) tip–atom terms: two terms per instruction -------------
+
+__device__ __forceinline__ float2 f2(float a) { return make_float2(a, a); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+
+// Tip position broadcast to both components.  Separations use the high
+// word of the double-float position only: the atoms are FP32-rounded, so the
+// low word (< half an FP32 ulp of the position) adds nothing to the accuracy
+// of a separation; it still carries the position update between steps.
+struct Tip2 {
+    float2 hx, hy, hz;
+};
+
+// Sums of one chunk: negated forces and the energy, per component.
+struct Sum2 {
+    float2 gx, gy, gz, e;
+};
+
+// Two terms of a TermPair32: LJ (interactions.cpp:15-27) or Morse (:29-40),
+// plus Coulomb (:42-51) when `coul`.  1/r comes from rsqrt.approx and LJ's
+// 1/r^2 is its square, which Coulomb reuses (qq/r^3 = (qq/r)(1/r^2)).
+// Accumulates -F and E into s.
+template <bool kMorse>
+__device__ __forceinline__ void unit32(const TermPair32& t, const Tip2& p, bool coul, Sum2& s) {
+    const float4 xy = t.xy, zq = t.zq, pa = t.pa;
+    const float2 dx = add2(p.hx, make_float2(xy.x, xy.y));   // tip - atom
+    const float2 dy = add2(p.hy, make_float2(xy.z, xy.w));
+    const float2 dz = add2(p.hz, make_float2(zq.x, zq.y));
+    const float2 r2 = fma2(dx, dx, fma2(dy, dy, mul2(dz, dz)));
+    const float2 ir = make_float2(rsqrt_fast(r2.x), rsqrt_fast(r2.y));
+    float2 nfs, e;
+    if (!kMorse) {
+        const float2 ir2 = mul2(ir, ir);
+        const float2 ir6 = mul2(mul2(ir2, ir2), ir2);
+        const float2 nt6 = mul2(make_float2(pa.x, pa.y), ir6);            // -es6/r^6
+        const float2 t12 = mul2(mul2(make_float2(pa.z, pa.w), ir6), ir6);  // es12/r^12
+        e = add2(t12, nt6);
+        nfs = mul2(fma2(f2(-12.f), t12, mul2(f2(-6.f), nt6)), ir2);
+        if (coul) {
+            const float2 nec = mul2(make_float2(zq.z, zq.w), ir);          // -qq/r
+            nfs = fma2(nec, ir2, nfs);
+            e = fma2(nec, f2(-1.f), e);
+        }
+    } else {
+        const float4 pb = t.pb;
+        const float2 r = mul2(r2, ir);
+        const float2 arg = mul2(make_float2(pa.z, pa.w), add2(r, make_float2(pb.x, pb.y)));
+        const float2 d = make_float2(__expf(arg.x), __expf(arg.y));
+        const float2 dm1 = add2(d, f2(-1.f));
+        e = mul2(mul2(make_float2(pa.x, pa.y), dm1), dm1);
+        nfs = mul2(mul2(mul2(make_float2(pb.z, pb.w), d), dm1), ir);
+        if (coul) {
+            const float2 nec = mul2(make_float2(zq.z, zq.w), ir);
+            nfs = fma2(mul2(nec, ir), ir, nfs);
+            e = fma2(nec, f2(-1.f), e);
+        }
+    }
+    s.gx = fma2(nfs, dx, s.gx);
+    s.gy = fma2(nfs, dy, s.gy);
+    s.gz = fma2(nfs, dz, s.gz);
+    s.e = add2(s.e, e);
+}
+
+// Units [begin, end) of one kind: lane lg of the group takes begin + lg,
+// begin + lg + G, ...; kChunk / 2 units (kChunk terms) are summed plainly
+// before one compensated add.  Full chunks run without bounds tests.
+template <int G, bool kMorse>
+__device__ __forceinline__ void sum_units(const TermPair32* units, int begin, int end, int lg,
+                                          const Tip2& tp, bool coul, Acc& acc) {
+    constexpr int kUnits = kChunk / 2;
+    int u0 = begin + lg;
+    for (; u0 + (kUnits - 1) * G < end; u0 += G * kUnits) {
+        Sum2 sm;
+        sm.gx = sm.gy = sm.gz = sm.e = f2(0.f);
+#pragma unroll
+        for (int c = 0; c < kUnits; ++c) unit32<kMorse>(units[u0 + c * G], tp, coul, sm);
+        const float v[4] = {-(sm.gx.x + sm.gx.y), -(sm.gy.x + sm.gy.y), -(sm.gz.x + sm.gz.y),
+                            sm.e.x + sm.e.y};
+        acc.add(v);
+    }
+    if (u0 < end) {
+        Sum2 sm;
+        sm.gx = sm.gy = sm.gz = sm.e = f2(0.f);
+#pragma unroll
+        for (int c = 0; c < kUnits - 1; ++c)
+            if (u0 + c * G < end) unit32<kMorse>(units[u0 + c * G], tp, coul, sm);
+        const float v[4] = {-(sm.gx.x + sm.gx.y), -(sm.gy.x + sm.gy.y), -(sm.gz.x + sm.gz.y),
+                            sm.e.x + sm.e.y};
+        acc.add(v);
+    }
+}
+
 // FP32 view of a trilinear grid (ForceGrid, force_grid.hpp:15-51), converted
 // from the FP64 GridView once per scan: reciprocal steps (orthogonal) or the
 // inverse basis, and the origin split into hi + lo floats.
@@ -398,9 +492,8 @@ __device__ __forceinline__ bool mbar_try_wait(uint32_t mbar, uint32_t phase) {
 
 // Bulk-copy `bytes` (multiple of 16) of terms into the warp's slice; all lanes
 // wait on the warp's mbarrier with a bounded spin.  Returns false on timeout.
-__device__ bool stage_terms(WarpHdr* hdr, AtomRec32* dst, const AtomRec32* src, int n,
+__device__ bool stage_terms(WarpHdr* hdr, void* dst, const void* src, uint32_t bytes,
                             uint32_t& phase, int lane) {
-    const uint32_t bytes = (uint32_t)n * (uint32_t)sizeof(AtomRec32);
     const uint32_t mbar = smem_addr(&hdr->mbar);
     __syncwarp();
     if (lane == 0) {
@@ -490,8 +583,8 @@ __global__ void __launch_bounds__(256) relax32_kernel(const BatchScan* __restric
     long long pending = -1;       // next tile, of another scan
     bool exhausted = false;
     const BatchScan* S = nullptr;
-    const AtomRec32* terms = nullptr;
-    int n_terms = 0;
+    const TermPair32* units = nullptr;
+    int n_units = 0, n_units_lj = 0;
     bool coul = false;
     int pairs_per_eval = 0;
     mafm_point* out = nullptr;
@@ -606,22 +699,25 @@ __global__ void __launch_bounds__(256) relax32_kernel(const BatchScan* __restric
                 t_next = B.col_begin + (int)(pending - B.tile_begin) * cols_per_tile;
                 t_end = min(B.col_end, t_next + cols_per_tile);
                 pending = -1;
-                n_terms = B.p.n_terms_direct;
+                // rigid-grid scans evaluate no direct terms
+                n_units = B.p.n_terms_direct > 0 ? B.p.n_units : 0;
+                n_units_lj = B.p.n_terms_direct > 0 ? B.p.n_units_lj : 0;
                 coul = B.has_coulomb != 0;
                 pairs_per_eval = B.n_pairs_per_eval;
                 out = B.out;
                 __syncwarp();
                 if (lane == 0) make_warp_params(B, hdr->wp);
                 __syncwarp();
-                if (n_terms > 0 && n_terms <= smem_terms) {
-                    if (!stage_terms(hdr, sm_terms, B.p.atoms32, n_terms, phase, lane)) {
+                if (n_units > 0 && 2 * n_units <= smem_terms) {
+                    if (!stage_terms(hdr, sm_terms, B.p.units32,
+                                     (uint32_t)n_units * (uint32_t)sizeof(TermPair32), phase, lane)) {
                         err |= ERR_STAGE_TIMEOUT;
                         alive = false;
                         break;
                     }
-                    terms = sm_terms;
+                    units = reinterpret_cast<const TermPair32*>(sm_terms);
                 } else {
-                    terms = B.p.atoms32;
+                    units = B.p.units32;
                 }
                 if (g.col == -2) g.col = -1;   // groups that found nothing may retry
                 continue;
@@ -639,22 +735,12 @@ __global__ void __launch_bounds__(256) relax32_kernel(const BatchScan* __restric
         Acc acc;
         acc.zero();
         {
-            const DF ex = g.ex, ey = g.ey, ez = g.ez;
-            for (int j0 = lg; j0 < n_terms; j0 += G * kChunk) {
-                float v[4] = {0.f, 0.f, 0.f, 0.f};
-#pragma unroll
-                for (int u = 0; u < kChunk; ++u) {
-                    const int j = j0 + u * G;
-                    if (j < n_terms) {
-                        const AtomRec32 t = terms[j];
-                        const float dx = (ex.hi - t.a.x) + ex.lo;
-                        const float dy = (ey.hi - t.a.y) + ey.lo;
-                        const float dz = (ez.hi - t.a.z) + ez.lo;
-                        pair32(t, dx, dy, dz, coul, v);
-                    }
-                }
-                acc.add(v);
-            }
+            Tip2 tp;
+            tp.hx = f2(g.ex.hi);
+            tp.hy = f2(g.ey.hi);
+            tp.hz = f2(g.ez.hi);
+            sum_units<G, false>(units, 0, n_units_lj, lg, tp, coul, acc);
+            sum_units<G, true>(units, n_units_lj, n_units, lg, tp, coul, acc);
         }
         if (G > 1) acc.template group_reduce<G>();
 
@@ -813,7 +899,10 @@ __global__ void __launch_bounds__(256) relax32_kernel(const BatchScan* __restric
                     // taken between double-float totals
                     const float ediff = (SE.hi - g.e_last.hi) + (SE.lo - g.e_last.lo);
                     g.e_last = SE;
-                    const float fl = sqrtf(SFx * SFx + SFy * SFy + SFz * SFz);
+                    // |F| and 1/|F| from one rsqrt (no IEEE sqrt or divide in the slot)
+                    const float f2s = SFx * SFx + SFy * SFy + SFz * SFz;
+                    const float irf = rsqrt_fast(f2s);
+                    const float fl = f2s > 1e-30f ? f2s * irf : 0.f;
                     bool conv;
                     if (W.minterm == MAFM_TERM_E) conv = fabsf(ediff) < W.etol;
                     else if (W.minterm == MAFM_TERM_F) conv = fl < W.ftol;
@@ -832,10 +921,10 @@ __global__ void __launch_bounds__(256) relax32_kernel(const BatchScan* __restric
                             const float pw = wx * SFx + wy * SFy + wz * SFz;
                             float hx2 = 0.f, hy2 = 0.f, hz2 = 0.f;
                             if (fl > 1e-10f) {
-                                const float inv = 1.f / fl;
-                                hx2 = SFx * inv; hy2 = SFy * inv; hz2 = SFz * inv;
+                                hx2 = SFx * irf; hy2 = SFy * irf; hz2 = SFz * irf;
                             }
-                            const float vl = sqrtf(wx * wx + wy * wy + wz * wz);
+                            const float w2 = wx * wx + wy * wy + wz * wz;
+                            const float vl = w2 > 1e-30f ? w2 * rsqrt_fast(w2) : 0.f;
                             const float a = g.alpha, b = 1.f - a;
                             g.vx = b * wx + a * hx2 * vl;
                             g.vy = b * wy + a * hy2 * vl;
@@ -918,14 +1007,15 @@ __global__ void sample32_kernel(const ScanParams p, int what, const double* pts,
 // one thread per node, terms staged through shared memory in tiles shared by
 // the whole block (all threads read the same term: broadcast).
 
-constexpr int kBuildTile = 2048;   // terms per shared-memory tile (64 KB)
+constexpr int kBuildUnits = 1024;  // paired-term records per shared-memory tile (64 KB)
 
 __global__ void __launch_bounds__(256) grid_build32_kernel(const ScanParams p, const GridView g,
                                                            float4* out, RunCounters* ctr) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
-    AtomRec32* tile = reinterpret_cast<AtomRec32*>(smem_raw);
+    TermPair32* tile = reinterpret_cast<TermPair32*>(smem_raw);
     const long long total = (long long)g.n[0] * g.n[1] * g.n[2];
-    const int n = p.n_terms_direct;
+    const int n = p.n_terms_direct > 0 ? p.n_units : 0;
+    const int n_lj = p.n_terms_direct > 0 ? p.n_units_lj : 0;
     const bool coul = p.has_coulomb != 0;
     unsigned err = 0;
     for (long long base = (long long)blockIdx.x * blockDim.x; base < total;
@@ -945,24 +1035,20 @@ __global__ void __launch_bounds__(256) grid_build32_kernel(const ScanParams p, c
         }
         Acc acc;
         acc.zero();
-        for (int t0 = 0; t0 < n; t0 += kBuildTile) {
-            const int cnt = min(kBuildTile, n - t0);
+        Tip2 tp;
+        tp.hx = f2(tx.hi);
+        tp.hy = f2(ty.hi);
+        tp.hz = f2(tz.hi);
+        // the paired terms in shared tiles of kBuildUnits records, read by the
+        // whole block (broadcast); LJ records, then Morse records
+        for (int t0 = 0; t0 < n; t0 += kBuildUnits) {
+            const int cnt = min(kBuildUnits, n - t0);
             __syncthreads();
-            for (int q = threadIdx.x; q < cnt; q += blockDim.x) tile[q] = p.atoms32[t0 + q];
+            for (int q = threadIdx.x; q < cnt; q += blockDim.x) tile[q] = p.units32[t0 + q];
             __syncthreads();
-            for (int j0 = 0; j0 < cnt; j0 += kChunk) {
-                float v[4] = {0, 0, 0, 0};
-#pragma unroll
-                for (int u = 0; u < kChunk; ++u) {
-                    const int j = j0 + u;
-                    if (j < cnt) {
-                        const AtomRec32 t = tile[j];
-                        pair32(t, (tx.hi - t.a.x) + tx.lo, (ty.hi - t.a.y) + ty.lo,
-                               (tz.hi - t.a.z) + tz.lo, coul, v);
-                    }
-                }
-                acc.add(v);
-            }
+            const int lj_end = min(max(n_lj - t0, 0), cnt);
+            sum_units<1, false>(tile, 0, lj_end, 0, tp, coul, acc);
+            sum_units<1, true>(tile, lj_end, cnt, 0, tp, coul, acc);
         }
         if (valid) {
             if (p.es.g32) {
@@ -1041,7 +1127,7 @@ cudaError_t launch_sample32(const ScanParams& p, int what, const double* pts, in
 
 cudaError_t launch_grid_build32(const ScanParams& p, const GridView& g, float4* out,
                                 RunCounters* ctr, cudaStream_t s) {
-    const size_t smem = (size_t)kBuildTile * sizeof(AtomRec32);
+    const size_t smem = (size_t)kBuildUnits * sizeof(TermPair32);
     cudaError_t e = cudaFuncSetAttribute(grid_build32_kernel,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;

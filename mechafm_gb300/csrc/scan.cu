@@ -207,6 +207,7 @@ struct mafm_scan {
     mafm::ScanParams P{};               // shared parameters; pointers filled per precision
     mafm::DevBuf<mafm::AtomRec64> atoms64;
     mafm::DevBuf<mafm::AtomRec32> atoms32;
+    mafm::DevBuf<mafm::TermPair32> units32;
     mafm::DevBuf<mafm::Node64> es64, grid64;
     mafm::DevBuf<float4> es32, grid32;
     mafm::GridView es_view{}, grid_view{};
@@ -311,6 +312,51 @@ void pack_terms(mafm_scan& s, const mafm_scan_desc& d) {
             t32.push_back(q);
             n_coul += r.coul;
         }
+    // Paired copy for the packed relax loop (TermPair32).
+    std::vector<TermPair32> u32;
+    int n_units_lj = 0;
+    for (int pass = 0; pass < 2; ++pass) {
+        std::vector<const AtomRec64*> run;
+        for (const AtomRec64& r : t64)
+            if ((pass == 0) == (r.kind == MAFM_PAIR_LJ)) run.push_back(&r);
+        for (size_t i = 0; i < run.size(); i += 2) {
+            const AtomRec64* t[2] = {run[i], i + 1 < run.size() ? run[i + 1] : nullptr};
+            float f[16];
+            for (int c = 0; c < 2; ++c) {
+                AtomRec64 z{};
+                z.x = z.y = z.z = 1.0e4;   // padding: zero parameters, far away
+                const AtomRec64& r = t[c] ? *t[c] : z;
+                f[0 + c] = (float)-r.x;
+                f[2 + c] = (float)-r.y;
+                f[4 + c] = (float)-r.z;
+                f[6 + c] = (float)-r.qq;
+                if (pass == 0) {
+                    f[8 + c] = (float)-r.p0;
+                    f[10 + c] = (float)r.p1;
+                    f[12 + c] = 0.f;
+                    f[14 + c] = 0.f;
+                } else {
+                    f[8 + c] = (float)r.p0;
+                    f[10 + c] = (float)-r.p1;
+                    f[12 + c] = (float)-r.p2;
+                    f[14 + c] = (float)(-2.0 * r.p0 * r.p1);
+                }
+            }
+            TermPair32 q;
+            q.xy = make_float4(f[0], f[1], f[2], f[3]);
+            q.zq = make_float4(f[4], f[5], f[6], f[7]);
+            q.pa = make_float4(f[8], f[9], f[10], f[11]);
+            q.pb = make_float4(f[12], f[13], f[14], f[15]);
+            u32.push_back(q);
+        }
+        if (pass == 0) n_units_lj = (int)u32.size();
+    }
+    s.units32.alloc(std::max<size_t>(u32.size(), 1));
+    if (!u32.empty())
+        cuda_check(cudaMemcpy(s.units32.p, u32.data(), u32.size() * sizeof(TermPair32),
+                              cudaMemcpyHostToDevice), "upload terms");
+    s.P.n_units = (int)u32.size();
+    s.P.n_units_lj = n_units_lj;
     s.atoms64.alloc(std::max<size_t>(t64.size(), 1));
     s.atoms32.alloc(std::max<size_t>(t32.size(), 1));
     if (!t64.empty()) {
@@ -571,7 +617,10 @@ Relax32Config default_config(long long n_cols, int max_terms, const mafm_run_opt
     if (max_terms <= 1) G = 1;
     c.lanes = (o && o->lanes_per_column) ? o->lanes_per_column : G;
     c.cols_per_tile = (o && o->columns_per_tile) ? o->columns_per_tile : 32 / c.lanes;
-    c.smem_terms = std::min(std::max(max_terms, 1), 256);
+    // Shared slice per warp, in 32 B term slots: the paired records of up to
+    // 400 terms (each kind's run padded to even: + 2); 12.9 KB per warp keeps
+    // two 8-warp blocks per SM.
+    c.smem_terms = std::min(std::max(max_terms, 1) + 2, 402);
     c.smem_terms = (c.smem_terms + 1) & ~1;
     c.blocks = 0;
     // Persistent-kernel time limit; MAFM_WATCHDOG_S overrides the 120 s default.
@@ -609,6 +658,7 @@ int mafm_scan_create(int device, const mafm_scan_desc* desc, mafm_scan** out) {
             pack_terms(*s, d);
             P.atoms64 = s->atoms64.p;
             P.atoms32 = s->atoms32.p;
+            P.units32 = s->units32.p;
             P.ts_mode = d.rigidgrid ? 2 : (d.use_external_potential ? 1 : 0);
             P.td_kind = d.dummy_pair.kind;
             for (int k = 0; k < 3; ++k) P.td_p[k] = d.dummy_pair.p[k];
