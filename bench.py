@@ -17,8 +17,8 @@ One step = one relaxation of every point by the FP32-compensated persistent
 kernel, launched from a prepared plan (mafm_plan_launch) captured in a CUDA
 graph; launch shape (lanes per column, block, tile) from mafm_autotune.
 `value` = points/s with inputs resident and outputs in HBM; `e2e` = the same
-through the C ABI from host memory (scan creation with the upload, relax, D2H
-of every point).  The plain FP64 kernel runs on a subset for the FP32/FP64
+through the C ABI from host memory (scan creation with the upload, relax, and
+every point record delivered into pinned host memory).  The plain FP64 kernel runs on a subset for the FP32/FP64
 speed-up and the FP32C error against it.  The CPU baseline is the oracle port
 (FP64, OpenMP on every host thread) on a sample of about ten seconds: centre
 column blocks of every scan, or for rigid-grid scans a centre crop whose
@@ -351,13 +351,22 @@ def fp64_compare(scans, descs, value, dev):
         jobs = [(s, 0, 0) for s in scans[:3]]
         subset = "the first 3 scans"
     p64s, p32s, ms64, npts = [], [], 0.0, 0
+    ms_build64 = 0.0
     for s, a, b in jobs:
+        if s.desc.c.rigidgrid:
+            # the FP64 grid build of the crop, timed on its own
+            stream = torch.cuda.current_stream(dev)
+            sp = C.c_void_p(stream.cuda_stream)
+            _abi.check(_abi.lib().mafm_scan_build_grid(s.handle, _abi.FP64, sp))
+            ms_build64 = time_events(stream, lambda: _abi.check(
+                _abi.lib().mafm_scan_build_grid(s.handle, _abi.FP64, sp)))
         p64, s64 = s.run(_abi.FP64, col_begin=a, col_end=b)
         p32, _ = s.run(_abi.FP32C, col_begin=a, col_end=b)
         p64s.append(p64)
         p32s.append(p32)
         ms64 += s64.kernel_ms
         npts += len(p64)
+    crop_nodes = rigid_nodes(owned[0].desc.c) if owned else 0
     for s in owned:
         s.close()
     p64 = np.concatenate(p64s)
@@ -365,8 +374,17 @@ def fp64_compare(scans, descs, value, dev):
     tip_err = np.abs(p32["tip"] - p64["tip"]).max(axis=1)
     fz = np.abs(p32["force"][:, 2] - p64["force"][:, 2]) / np.maximum(np.abs(p64["force"][:, 2]), 0.01)
     rate64 = npts / (ms64 / 1000.0)
+    extra = {}
+    if owned:
+        # a rigid-grid step is grid build + relax: scale the crop's FP64 build
+        # by grid nodes and its relax by points, as the FP32C step does both
+        d = descs[0]
+        t64 = (ms_build64 * rigid_nodes(d.c) / crop_nodes + ms64 * d.n_points / npts) / 1000.0
+        rate64 = d.n_points / t64
+        extra = {"grid_build_ms_crop": ms_build64, "relax_ms_crop": ms64,
+                 "scaled_to": "full scan: build by grid nodes, relax by points"}
     return {
-        "points_per_s": rate64, "points": npts, "subset": subset, "kernel_ms": ms64,
+        "points_per_s": rate64, "points": npts, "subset": subset, "kernel_ms": ms64, **extra,
         "fp32c_speedup": value / rate64,
         "tip_err_A": {"max": float(tip_err.max()), "p99_9": float(np.percentile(tip_err, 99.9)),
                       "median": float(np.median(tip_err)),
@@ -545,8 +563,8 @@ def ours(args, rank, world, local):
             with torch.cuda.stream(stream):
                 torch.sub(fz_view, target, out=wbuf)
                 wbuf.mul_(2.0 / n_pts)
-            _abi.check(L.mafm_adjoint(scans[0].handle, C.c_void_p(outs[0].data_ptr()),
-                                      C.c_void_p(wbuf.data_ptr()), C.byref(grads), sptr))
+            _abi.check(L.mafm_adjoint_ex(scans[0].handle, _abi.FP32C, C.c_void_p(outs[0].data_ptr()),
+                                         C.c_void_p(wbuf.data_ptr()), C.byref(grads), sptr))
 
     for _ in range(args.warmup):
         build()
@@ -627,7 +645,9 @@ def ours(args, rank, world, local):
         h2d += n_pts * (64 + 8)
         d2h = n_pts * 64
     else:
-        host = [np.zeros(d.n_points, dtype=_abi.POINT_DTYPE) for d in descs]
+        # pinned host buffers for the results (written by the kernel directly)
+        pinned = [torch.empty(d.n_points * 64, dtype=torch.uint8, pin_memory=True) for d in descs]
+        host = [p.numpy().view(_abi.POINT_DTYPE) for p in pinned]
         e2e_opts = _abi.RunOpts(_abi.FP32C, used.lanes_per_column, used.block_threads,
                                 used.columns_per_tile, 0, 0)
         for i in range(reps + 1):   # the first pass warms up
@@ -680,9 +700,9 @@ def ours(args, rank, world, local):
                 "kernel": "grid_build32_kernel", "kernel_ms": ms_build, "nodes": nodes,
                 "flops_per_node": float(gflops / nodes)})))
         if adjoint:
-            rooflines.append((ms_adj, {"kernel": "adjoint_kernel (FP64)", "kernel_ms": ms_adj,
-                                       "bound": "fp64", "note": "FP64 Jacobian and parameter "
-                                       "derivatives per point; not the dominant kernel"}))
+            rooflines.append((ms_adj, {"kernel": "adjoint32_kernel (FP32C)", "kernel_ms": ms_adj,
+                                       "bound": "fp32", "note": "FP32 per-term Jacobians and "
+                                       "parameter derivatives, FP64 3x3 solve per point"}))
         rooflines.sort(key=lambda r: -r[0])
         threads = cpu_threads()
         if args.cpu_seconds > 0:

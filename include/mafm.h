@@ -198,14 +198,17 @@ int mafm_scan_size(const mafm_scan* scan, int64_t* n_points, int64_t* n_columns)
  * (simulation.cpp:78-122) with FIREMinimisation / SDMinimisation
  * (minimiser.cpp:39-129), the integrators (integrators.cpp:8-111) and
  * System::getOutput (system.cpp:28-51).  `out` holds n_points records and
- * may be host or device memory; for host memory the call copies the result
- * back and returns after the copy.  `stats` may be NULL; when given, the
- * call synchronises the stream. */
+ * may be host or device memory; for host memory the call returns when the
+ * points are there.  Pinned (page-locked) host memory is written by the
+ * kernel directly; pageable memory goes through a device staging buffer and
+ * one copy.  `stats` may be NULL; when given, the call synchronises the
+ * stream. */
 int mafm_run(mafm_scan* scan, const mafm_run_opts* opts, mafm_point* out,
              mafm_run_stats* stats, void* stream);
 
 /* Relax several scans in one persistent launch (MAFM_FP32C only).  outs[s]
- * receives scan s's points; all outs must be device memory, or all host. */
+ * receives scan s's points; all outs must be device memory, or all host
+ * (pinned host outputs are written directly, as for mafm_run). */
 int mafm_run_batch(mafm_scan* const* scans, int32_t n_scans, const mafm_run_opts* opts,
                    mafm_point* const* outs, mafm_run_stats* stats, void* stream);
 
@@ -273,6 +276,12 @@ typedef struct mafm_grad {
 } mafm_grad;
 int mafm_adjoint(mafm_scan* scan, const mafm_point* pts, const double* dl_dfz, mafm_grad* out,
                  void* stream);
+/* mafm_adjoint with a precision: MAFM_FP64 (the same as mafm_adjoint) or
+ * MAFM_FP32C (per-term Jacobians and parameter derivatives in FP32 with
+ * compensated sums, the per-point 3x3 solve in FP64; gradients agree with
+ * the FP64 ones to about 1e-5 relative).  No counterpart in the reference. */
+int mafm_adjoint_ex(mafm_scan* scan, int32_t precision, const mafm_point* pts,
+                    const double* dl_dfz, mafm_grad* out, void* stream);
 
 /* ---- frequency-shift images ------------------------------------------------
  * The reference's post-processing (simple-vafm-image.py:77-89, 204) turns Fz

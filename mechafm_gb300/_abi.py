@@ -113,6 +113,7 @@ SIGNATURES = {
     "mafm_autotune": (C.c_int, [C.POINTER(_P), C.c_int32, C.POINTER(RunOpts),
                                 C.POINTER(C.c_double), _P]),
     "mafm_adjoint": (C.c_int, [_P, _P, _P, C.POINTER(Grad), _P]),
+    "mafm_adjoint_ex": (C.c_int, [_P, C.c_int32, _P, _P, C.POINTER(Grad), _P]),
     "mafm_df_weights": (C.c_int, [C.POINTER(DfParams), C.c_double, _P, C.c_int32,
                                   C.POINTER(C.c_int32), C.POINTER(C.c_double)]),
     "mafm_df": (C.c_int, [_P, C.c_int64, C.c_int32, C.c_int32, C.c_int32, C.c_double,

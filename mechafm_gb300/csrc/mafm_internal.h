@@ -89,7 +89,7 @@ struct __align__(16) TermPair32 {
     float4 xy;             // -x0, -x1, -y0, -y1
     float4 zq;             // -z0, -z1, -qq0, -qq1
     float4 pa;             // LJ -es6_0, -es6_1, es12_0, es12_1 | Morse De_0, De_1, -a_0, -a_1
-    float4 pb;             // Morse -re_0, -re_1, -2 De a_0, -2 De a_1 (zero for LJ)
+    float4 pb;             // LJ -12 es12_0, -12 es12_1, 6 es6_0, 6 es6_1 | Morse -re_0, -re_1, -2 De a_0, -2 De a_1
 };
 
 // A trilinear force grid (ForceGrid, force_grid.hpp:15-51).
@@ -184,9 +184,9 @@ cudaError_t launch_sample32(const ScanParams& p, int what, const double* pts, in
 cudaError_t launch_grid_build32(const ScanParams& p, const GridView& g, float4* out,
                                 RunCounters* ctr, cudaStream_t s);
 int sm_count();
-cudaError_t launch_adjoint(const ScanParams& p, const mafm_point* pts, const double* w,
-                           long long n_points, double qbase_qtip, double* gterm, RunCounters* ctr,
-                           cudaStream_t s);
+cudaError_t launch_adjoint(const ScanParams& p, int precision, const int* index32,
+                           const mafm_point* pts, const double* w, long long n_points,
+                           double qbase_qtip, double* gterm, RunCounters* ctr, cudaStream_t s);
 
 }  // namespace mafm
 

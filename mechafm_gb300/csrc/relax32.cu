@@ -168,33 +168,30 @@ struct Sum2 {
     float2 gx, gy, gz, e;
 };
 
-// Two terms of a TermPair32: LJ (interactions.cpp:15-27) or Morse (:29-40),
-// plus Coulomb (:42-51) when `coul`.  1/r comes from rsqrt.approx and LJ's
-// 1/r^2 is its square, which Coulomb reuses (qq/r^3 = (qq/r)(1/r^2)).
+// Two terms of a TermPair32 at one tip position, given the separation
+// d = tip - atom and dx^2 + dy^2: LJ (interactions.cpp:15-27) or Morse
+// (:29-40), plus Coulomb (:42-51) when `coul`.  1/r comes from rsqrt.approx
+// and LJ's 1/r^2 is its square, which Coulomb reuses (qq/r^3 = (qq/r)/r^2).
 // Accumulates -F and E into s.
 template <bool kMorse>
-__device__ __forceinline__ void unit32(const TermPair32& t, const Tip2& p, bool coul, Sum2& s) {
-    const float4 xy = t.xy, zq = t.zq, pa = t.pa;
-    const float2 dx = add2(p.hx, make_float2(xy.x, xy.y));   // tip - atom
-    const float2 dy = add2(p.hy, make_float2(xy.z, xy.w));
-    const float2 dz = add2(p.hz, make_float2(zq.x, zq.y));
-    const float2 r2 = fma2(dx, dx, fma2(dy, dy, mul2(dz, dz)));
+__device__ __forceinline__ void unit32_at(const TermPair32& t, float2 dx, float2 dy, float2 dxy2,
+                                          float2 dz, bool coul, Sum2& s) {
+    const float4 zq = t.zq, pa = t.pa, pb = t.pb;
+    const float2 r2 = fma2(dz, dz, dxy2);
     const float2 ir = make_float2(rsqrt_fast(r2.x), rsqrt_fast(r2.y));
     float2 nfs, e;
     if (!kMorse) {
+        // E = r^-6 (es12 r^-6 - es6), -F/d = r^-8 (6 es6 - 12 es12 r^-6)
         const float2 ir2 = mul2(ir, ir);
         const float2 ir6 = mul2(mul2(ir2, ir2), ir2);
-        const float2 nt6 = mul2(make_float2(pa.x, pa.y), ir6);            // -es6/r^6
-        const float2 t12 = mul2(mul2(make_float2(pa.z, pa.w), ir6), ir6);  // es12/r^12
-        e = add2(t12, nt6);
-        nfs = mul2(fma2(f2(-12.f), t12, mul2(f2(-6.f), nt6)), ir2);
+        e = mul2(ir6, fma2(make_float2(pa.z, pa.w), ir6, make_float2(pa.x, pa.y)));
+        nfs = mul2(mul2(ir6, ir2), fma2(make_float2(pb.x, pb.y), ir6, make_float2(pb.z, pb.w)));
         if (coul) {
             const float2 nec = mul2(make_float2(zq.z, zq.w), ir);          // -qq/r
             nfs = fma2(nec, ir2, nfs);
             e = fma2(nec, f2(-1.f), e);
         }
     } else {
-        const float4 pb = t.pb;
         const float2 r = mul2(r2, ir);
         const float2 arg = mul2(make_float2(pa.z, pa.w), add2(r, make_float2(pb.x, pb.y)));
         const float2 d = make_float2(__expf(arg.x), __expf(arg.y));
@@ -211,6 +208,16 @@ __device__ __forceinline__ void unit32(const TermPair32& t, const Tip2& p, bool 
     s.gy = fma2(nfs, dy, s.gy);
     s.gz = fma2(nfs, dz, s.gz);
     s.e = add2(s.e, e);
+}
+
+// Two terms of a TermPair32 at the tip position p.
+template <bool kMorse>
+__device__ __forceinline__ void unit32(const TermPair32& t, const Tip2& p, bool coul, Sum2& s) {
+    const float4 xy = t.xy, zq = t.zq;
+    const float2 dx = add2(p.hx, make_float2(xy.x, xy.y));   // tip - atom
+    const float2 dy = add2(p.hy, make_float2(xy.z, xy.w));
+    const float2 dz = add2(p.hz, make_float2(zq.x, zq.y));
+    unit32_at<kMorse>(t, dx, dy, fma2(dy, dy, mul2(dx, dx)), dz, coul, s);
 }
 
 // Units [begin, end) of one kind: lane lg of the group takes begin + lg,
@@ -239,6 +246,41 @@ __device__ __forceinline__ void sum_units(const TermPair32* units, int begin, in
         const float v[4] = {-(sm.gx.x + sm.gx.y), -(sm.gy.x + sm.gy.y), -(sm.gz.x + sm.gz.y),
                             sm.e.x + sm.e.y};
         acc.add(v);
+    }
+}
+
+// Units [begin, end) of one kind for NB tip positions that share x and y (a
+// strip of NB nodes of one grid column): the x and y separations and
+// dx^2 + dy^2 are computed once per record for all NB positions.
+template <bool kMorse, int NB>
+__device__ __forceinline__ void sum_units_strip(const TermPair32* units, int begin, int end,
+                                                float2 hx, float2 hy, const float2 (&hz)[NB],
+                                                bool coul, Acc (&acc)[NB]) {
+    constexpr int kUnits = kChunk / 2;
+    for (int u0 = begin; u0 < end; u0 += kUnits) {
+        Sum2 sm[NB];
+#pragma unroll
+        for (int n = 0; n < NB; ++n) sm[n].gx = sm[n].gy = sm[n].gz = sm[n].e = f2(0.f);
+#pragma unroll
+        for (int c = 0; c < kUnits; ++c) {
+            if (u0 + c < end) {
+                const TermPair32& t = units[u0 + c];
+                const float4 xy = t.xy, zq = t.zq;
+                const float2 dx = add2(hx, make_float2(xy.x, xy.y));
+                const float2 dy = add2(hy, make_float2(xy.z, xy.w));
+                const float2 dxy2 = fma2(dy, dy, mul2(dx, dx));
+                const float2 naz = make_float2(zq.x, zq.y);
+#pragma unroll
+                for (int n = 0; n < NB; ++n)
+                    unit32_at<kMorse>(t, dx, dy, dxy2, add2(hz[n], naz), coul, sm[n]);
+            }
+        }
+#pragma unroll
+        for (int n = 0; n < NB; ++n) {
+            const float v[4] = {-(sm[n].gx.x + sm[n].gx.y), -(sm[n].gy.x + sm[n].gy.y),
+                                -(sm[n].gz.x + sm[n].gz.y), sm[n].e.x + sm[n].e.y};
+            acc[n].add(v);
+        }
     }
 }
 
@@ -1008,37 +1050,45 @@ __global__ void sample32_kernel(const ScanParams p, int what, const double* pts,
 // the whole block (all threads read the same term: broadcast).
 
 constexpr int kBuildUnits = 1024;  // paired-term records per shared-memory tile (64 KB)
+constexpr int kStrip = 4;          // grid nodes of one column per thread
 
-__global__ void __launch_bounds__(256) grid_build32_kernel(const ScanParams p, const GridView g,
+__global__ void __launch_bounds__(256, 2) grid_build32_kernel(const ScanParams p, const GridView g,
                                                            float4* out, RunCounters* ctr) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     TermPair32* tile = reinterpret_cast<TermPair32*>(smem_raw);
-    const long long total = (long long)g.n[0] * g.n[1] * g.n[2];
+    // one thread per strip of kStrip consecutive nodes of a grid column (z fastest)
+    const int nzs = (g.n[2] + kStrip - 1) / kStrip;
+    const long long total = (long long)g.n[0] * g.n[1] * nzs;
     const int n = p.n_terms_direct > 0 ? p.n_units : 0;
     const int n_lj = p.n_terms_direct > 0 ? p.n_units_lj : 0;
     const bool coul = p.has_coulomb != 0;
     unsigned err = 0;
     for (long long base = (long long)blockIdx.x * blockDim.x; base < total;
          base += (long long)gridDim.x * blockDim.x) {
-        const long long idx = base + threadIdx.x;
-        const bool valid = idx < total;
-        DF tx{0, 0}, ty{0, 0}, tz{0, 0};
+        const long long sid = base + threadIdx.x;
+        const bool valid = sid < total;
+        DF tx{0, 0}, ty{0, 0}, tz[kStrip];
+        long long ij = 0;
+        int k0 = 0;
+        for (int q = 0; q < kStrip; ++q) tz[q] = DF{0, 0};
         if (valid) {
-            const int k = (int)(idx % g.n[2]);
-            const long long ij = idx / g.n[2];
+            k0 = (int)(sid % nzs) * kStrip;
+            ij = sid / nzs;
             const int j = (int)(ij % g.n[1]), i = (int)(ij / g.n[1]);
             double x, y;
             dummy_xy(p, p.tip_pbc != 0, i * g.basis[0] + g.origin[0], j * g.basis[4] + g.origin[1], x, y);
             tx = df_split(x);
             ty = df_split(y);
-            tz = df_split(k * g.basis[8] + g.origin[2]);
+            for (int q = 0; q < kStrip; ++q) tz[q] = df_split((k0 + q) * g.basis[8] + g.origin[2]);
         }
-        Acc acc;
-        acc.zero();
-        Tip2 tp;
-        tp.hx = f2(tx.hi);
-        tp.hy = f2(ty.hi);
-        tp.hz = f2(tz.hi);
+        Acc acc[kStrip];
+        float2 hz[kStrip];
+#pragma unroll
+        for (int q = 0; q < kStrip; ++q) {
+            acc[q].zero();
+            hz[q] = f2(tz[q].hi);
+        }
+        const float2 hx = f2(tx.hi), hy = f2(ty.hi);
         // the paired terms in shared tiles of kBuildUnits records, read by the
         // whole block (broadcast); LJ records, then Morse records
         for (int t0 = 0; t0 < n; t0 += kBuildUnits) {
@@ -1047,17 +1097,22 @@ __global__ void __launch_bounds__(256) grid_build32_kernel(const ScanParams p, c
             for (int q = threadIdx.x; q < cnt; q += blockDim.x) tile[q] = p.units32[t0 + q];
             __syncthreads();
             const int lj_end = min(max(n_lj - t0, 0), cnt);
-            sum_units<1, false>(tile, 0, lj_end, 0, tp, coul, acc);
-            sum_units<1, true>(tile, lj_end, cnt, 0, tp, coul, acc);
+            sum_units_strip<false, kStrip>(tile, 0, lj_end, hx, hy, hz, coul, acc);
+            sum_units_strip<true, kStrip>(tile, lj_end, cnt, hx, hy, hz, coul, acc);
         }
         if (valid) {
-            if (p.es.g32) {
-                float v[4] = {0, 0, 0, 0};
-                int unused = 0;
-                interp32(make_lookup(p.es), tx, ty, tz, v, unused, err);
-                acc.add(v);
+#pragma unroll
+            for (int q = 0; q < kStrip; ++q) {
+                if (k0 + q >= g.n[2]) break;
+                if (p.es.g32) {
+                    float v[4] = {0, 0, 0, 0};
+                    int unused = 0;
+                    interp32(make_lookup(p.es), tx, ty, tz[q], v, unused, err);
+                    acc[q].add(v);
+                }
+                out[ij * g.n[2] + k0 + q] =
+                    make_float4(acc[q].val(0), acc[q].val(1), acc[q].val(2), acc[q].val(3));
             }
-            out[idx] = make_float4(acc.val(0), acc.val(1), acc.val(2), acc.val(3));
         }
     }
     if (err) atomicOr(&ctr->error_word, err);
@@ -1131,7 +1186,7 @@ cudaError_t launch_grid_build32(const ScanParams& p, const GridView& g, float4* 
     cudaError_t e = cudaFuncSetAttribute(grid_build32_kernel,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    const long long total = (long long)g.n[0] * g.n[1] * g.n[2];
+    const long long total = (long long)g.n[0] * g.n[1] * ((g.n[2] + kStrip - 1) / kStrip);
     long long blocks = (total + 255) / 256;
     const long long cap = (long long)sm_count() * 8;
     if (blocks > cap) blocks = cap;

@@ -208,6 +208,7 @@ struct mafm_scan {
     mafm::DevBuf<mafm::AtomRec64> atoms64;
     mafm::DevBuf<mafm::AtomRec32> atoms32;
     mafm::DevBuf<mafm::TermPair32> units32;
+    mafm::DevBuf<int32_t> index32;       // FP64 term index of each atoms32 record
     mafm::DevBuf<mafm::Node64> es64, grid64;
     mafm::DevBuf<float4> es32, grid32;
     mafm::GridView es_view{}, grid_view{};
@@ -298,11 +299,13 @@ void pack_terms(mafm_scan& s, const mafm_scan_desc& d) {
         }
     // FP32 copy, LJ terms first so that lanes sharing a column rarely diverge on the kind.
     std::vector<AtomRec32> t32;
+    std::vector<int32_t> t32_index;   // FP64 term of each FP32 record
     t32.reserve(t64.size());
     int n_coul = 0;
     for (int pass = 0; pass < 2; ++pass)
         for (const AtomRec64& r : t64) {
             if ((pass == 0) != (r.kind == MAFM_PAIR_LJ)) continue;
+            t32_index.push_back((int32_t)(&r - t64.data()));
             AtomRec32 q;
             q.a = make_float4((float)r.x, (float)r.y, (float)r.z, (float)r.qq);
             int kind = r.kind;
@@ -333,8 +336,8 @@ void pack_terms(mafm_scan& s, const mafm_scan_desc& d) {
                 if (pass == 0) {
                     f[8 + c] = (float)-r.p0;
                     f[10 + c] = (float)r.p1;
-                    f[12 + c] = 0.f;
-                    f[14 + c] = 0.f;
+                    f[12 + c] = (float)(-12.0 * r.p1);
+                    f[14 + c] = (float)(6.0 * r.p0);
                 } else {
                     f[8 + c] = (float)r.p0;
                     f[10 + c] = (float)-r.p1;
@@ -359,7 +362,10 @@ void pack_terms(mafm_scan& s, const mafm_scan_desc& d) {
     s.P.n_units_lj = n_units_lj;
     s.atoms64.alloc(std::max<size_t>(t64.size(), 1));
     s.atoms32.alloc(std::max<size_t>(t32.size(), 1));
+    s.index32.alloc(std::max<size_t>(t32.size(), 1));
     if (!t64.empty()) {
+        cuda_check(cudaMemcpy(s.index32.p, t32_index.data(), t32_index.size() * sizeof(int32_t),
+                              cudaMemcpyHostToDevice), "upload terms");
         cuda_check(cudaMemcpy(s.atoms64.p, t64.data(), t64.size() * sizeof(AtomRec64),
                               cudaMemcpyHostToDevice), "upload terms");
         cuda_check(cudaMemcpy(s.atoms32.p, t32.data(), t32.size() * sizeof(AtomRec32),
@@ -596,6 +602,19 @@ bool is_device_ptr(const void* p) {
     return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
 }
 
+// Device-visible address of pinned (page-locked) host memory, or nullptr for
+// anything else.  Kernels write points straight into such buffers (over the
+// host link while they run), so no staging buffer and no copy are needed.
+mafm_point* pinned_view(void* p) {
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (a.type != cudaMemoryTypeHost || !a.devicePointer) return nullptr;
+    return static_cast<mafm_point*>(a.devicePointer);
+}
+
 void check_device_errors(const RunCounters& c) {
     if (c.error_word & ERR_GRID_INDEX)
         fail(MAFM_E_RANGE, "Invalid grid point: the tip left the rigid force grid "
@@ -733,9 +752,13 @@ int mafm_run(mafm_scan* scan, const mafm_run_opts* opts, mafm_point* out, mafm_r
             if (stats) *stats = mafm_run_stats{};
             return;
         }
+        // host outputs: pinned memory is written directly, pageable memory
+        // through the scan's device staging buffer
         const bool host_out = !is_device_ptr(out);
-        mafm_point* dout = out;
-        if (host_out) {
+        mafm_point* const pinned = host_out ? pinned_view(out) : nullptr;
+        const bool staged = host_out && !pinned;
+        mafm_point* dout = pinned ? pinned : out;
+        if (staged) {
             scan->stage.alloc(n_pts);
             dout = scan->stage.p;
         }
@@ -764,7 +787,7 @@ int mafm_run(mafm_scan* scan, const mafm_run_opts* opts, mafm_point* out, mafm_r
             cuda_check(launch_relax32(scan->batch.p, 1, n_tiles, cfg, scan->ctr.p, st), "relax32 launch");
         }
         cuda_check(cudaEventRecord(scan->ev1, st), "cudaEventRecord");
-        if (host_out)
+        if (staged)
             cuda_check(cudaMemcpyAsync(out, dout, n_pts * sizeof(mafm_point), cudaMemcpyDeviceToHost, st),
                        "copy points to host");
         if (stats || host_out) {
@@ -821,12 +844,19 @@ int mafm_run_batch(mafm_scan* const* scans, int32_t n_scans, const mafm_run_opts
         }
         Relax32Config cfg = default_config(total_cols, max_terms, opts);
         long long tiles = 0;
-        if (host_out) s0->stage.alloc(total_pts);
+        // host outputs: pinned ones are written directly, pageable ones staged
+        std::vector<mafm_point*> pinned((size_t)n_scans, nullptr);
+        bool any_staged = false;
+        for (int i = 0; i < n_scans && host_out; ++i) {
+            pinned[i] = pinned_view(outs[i]);
+            any_staged |= !pinned[i];
+        }
+        if (any_staged) s0->stage.alloc(total_pts);
         for (int i = 0; i < n_scans; ++i) {
             mafm_scan* s = scans[i];
             BatchScan& b = bs[i];
             b.p = build_params(*s);
-            b.out = host_out ? s0->stage.p + offsets[i] : outs[i];
+            b.out = !host_out ? outs[i] : pinned[i] ? pinned[i] : s0->stage.p + offsets[i];
             b.tile_begin = tiles;
             b.col_begin = 0;
             b.col_end = s->d.nx * s->d.ny;
@@ -845,6 +875,7 @@ int mafm_run_batch(mafm_scan* const* scans, int32_t n_scans, const mafm_run_opts
         cuda_check(cudaEventRecord(s0->ev1, st), "cudaEventRecord");
         if (host_out)
             for (int i = 0; i < n_scans; ++i) {
+                if (pinned[i]) continue;
                 const size_t np = (size_t)scans[i]->d.nx * scans[i]->d.ny * scans[i]->d.nz;
                 cuda_check(cudaMemcpyAsync(outs[i], s0->stage.p + offsets[i], np * sizeof(mafm_point),
                                            cudaMemcpyDeviceToHost, st), "copy points to host");
@@ -1171,8 +1202,15 @@ int mafm_autotune(mafm_scan* const* scans, int32_t n_scans, mafm_run_opts* best,
 
 extern "C" int mafm_adjoint(mafm_scan* scan, const mafm_point* pts, const double* dl_dfz,
                             mafm_grad* out, void* stream) {
+    return mafm_adjoint_ex(scan, MAFM_FP64, pts, dl_dfz, out, stream);
+}
+
+extern "C" int mafm_adjoint_ex(mafm_scan* scan, int32_t precision, const mafm_point* pts,
+                               const double* dl_dfz, mafm_grad* out, void* stream) {
     return guarded([&] {
         if (!scan || !pts || !dl_dfz || !out) fail(MAFM_E_INVALID, "null argument");
+        if (precision != MAFM_FP64 && precision != MAFM_FP32C)
+            fail(MAFM_E_INVALID, "unknown precision %d", precision);
         if (scan->d.rigidgrid)
             fail(MAFM_E_UNSUPPORTED, "gradients through a rigid force grid are not provided");
         cuda_check(cudaSetDevice(scan->device), "cudaSetDevice");
@@ -1199,7 +1237,8 @@ extern "C" int mafm_adjoint(mafm_scan* scan, const mafm_point* pts, const double
         cuda_check(cudaMemsetAsync(gterm.p, 0, (size_t)std::max(nt, 1) * 7 * sizeof(double), st), "memset");
         zero_counters(*scan, st);
         ScanParams p = build_params(*scan);
-        cuda_check(launch_adjoint(p, pp, pw, npts, scan->d.qbase * scan->d.tip_charge, gterm.p,
+        cuda_check(launch_adjoint(p, precision, scan->index32.p, pp, pw, npts,
+                                  scan->d.qbase * scan->d.tip_charge, gterm.p,
                                   scan->ctr.p, st), "adjoint launch");
         std::vector<double> g((size_t)std::max(nt, 1) * 7);
         cuda_check(cudaMemcpyAsync(g.data(), gterm.p, g.size() * sizeof(double), cudaMemcpyDeviceToHost, st),

@@ -190,9 +190,10 @@ class Scan:
                              C.byref(st) if st is not None else None, stream))
         return st
 
-    def adjoint(self, points: np.ndarray, dl_dfz: np.ndarray, stream=None) -> dict:
+    def adjoint(self, points: np.ndarray, dl_dfz: np.ndarray, stream=None,
+                precision=_abi.FP64) -> dict:
         """Gradients of L through the relaxation, given the relaxed points of a
-        run and dL/dFz per point (mafm_adjoint): dpos (n_atoms, 3), dcharge
+        run and dL/dFz per point (mafm_adjoint_ex): dpos (n_atoms, 3), dcharge
         (n_atoms,), dpair (n_types, 3) for tip_pair[t].p."""
         d = self.desc.c
         points = np.ascontiguousarray(points, dtype=_abi.POINT_DTYPE)
@@ -205,7 +206,7 @@ class Scan:
         g = _abi.Grad(dpos.ctypes.data_as(C.POINTER(C.c_double)),
                       dq.ctypes.data_as(C.POINTER(C.c_double)),
                       dpair.ctypes.data_as(C.POINTER(C.c_double)))
-        check(lib().mafm_adjoint(self._h, ptr(points), ptr(w), C.byref(g), stream))
+        check(lib().mafm_adjoint_ex(self._h, precision, ptr(points), ptr(w), C.byref(g), stream))
         return {"dpos": dpos, "dcharge": dq, "dpair": dpair}
 
     def sample(self, pts: np.ndarray, precision=_abi.FP64, what: int = 0) -> np.ndarray:

@@ -2,8 +2,8 @@
 
 `fz_image(desc, pos, charge, pair)` relaxes the scan on the GPU through the C
 ABI and returns the tip–surface Fz of every point as a tensor (nx, ny, nz);
-its backward calls mafm_adjoint (implicit differentiation at the relaxed
-points).  pos (n_atoms, 3) are the prepared surface positions, charge
+its backward calls mafm_adjoint_ex (implicit differentiation at the relaxed
+points) in the forward's precision.  pos (n_atoms, 3) are the prepared surface positions, charge
 (n_atoms,) the Coulomb charges, pair (n_types, 3) the tip pair parameters
 (LJ es6, es12, 0; Morse De, a, re).  Give pair as a function of per-type
 eps/sigma with `lj_pair_params` to get eps/sigma gradients by autograd.
@@ -27,9 +27,14 @@ class _FzImage(torch.autograd.Function):
                             charge.detach().cpu().double().numpy(),
                             pair.detach().cpu().double().numpy())
         scan = Scan(d, device=device)
-        pts, _ = scan.run(precision)
+        # pinned host records: the kernel writes them directly, and the
+        # backward's upload of them runs at the link's speed
+        buf = torch.empty(d.n_points * _abi.POINT_DTYPE.itemsize, dtype=torch.uint8, pin_memory=True)
+        pts, _ = scan.run(precision, out=buf.numpy().view(_abi.POINT_DTYPE))
+        ctx.buf = buf
         ctx.scan = scan
         ctx.pts = pts
+        ctx.precision = precision
         ctx.shapes = (pos.shape, charge.shape, pair.shape)
         ctx.dtypes = (pos.dtype, charge.dtype, pair.dtype)
         ctx.devices = (pos.device, charge.device, pair.device)
@@ -39,7 +44,7 @@ class _FzImage(torch.autograd.Function):
     @staticmethod
     def backward(ctx, grad_fz):
         w = grad_fz.detach().double().cpu().numpy().reshape(-1)
-        g = ctx.scan.adjoint(ctx.pts, w)
+        g = ctx.scan.adjoint(ctx.pts, w, precision=ctx.precision)
         out = []
         for key, shape, dt, dev in zip(("dpos", "dcharge", "dpair"), ctx.shapes, ctx.dtypes,
                                        ctx.devices):

@@ -176,3 +176,37 @@ def test_torch_autograd_matches_oracle(tmp_path):
     np.testing.assert_allclose(pos.grad.numpy(), want["dpos"], rtol=1e-8, atol=1e-12)
     np.testing.assert_allclose(chg.grad.numpy(), want["dcharge"], rtol=1e-8, atol=1e-12)
     np.testing.assert_allclose(pair.grad.numpy(), want["dpair"], rtol=1e-8, atol=1e-20)
+
+
+@pytest.mark.gpu
+def test_fp32c_adjoint_matches_oracle_adjoint(tmp_path):
+    """The FP32C adjoint (FP32 per-term work, FP64 3x3 solves) against the
+    oracle's FP64 adjoint on the same relaxed points: 1e-5 relative to the
+    largest gradient of each kind."""
+    desc = tight_cluster(tmp_path)
+    scan = Scan(desc, device=0)
+    pts, _ = scan.run(_abi.FP64)
+    w = np.random.default_rng(7).normal(size=len(pts))
+    g = scan.adjoint(pts, w, precision=_abi.FP32C)
+    want = oracle.adjoint(desc, pts, w)
+    for key in ("dpos", "dcharge", "dpair"):
+        scale = np.abs(want[key]).max()
+        np.testing.assert_allclose(g[key], want[key], rtol=0, atol=1e-5 * scale)
+
+
+@pytest.mark.gpu
+def test_fp32c_adjoint_matches_gpu_finite_differences(tmp_path):
+    desc = tight_cluster(tmp_path)
+    pert = Perturb(desc)
+    scan = Scan(desc, device=0)
+    pts, _ = scan.run(_abi.FP64)
+    w = np.random.default_rng(8).normal(size=len(pts))
+    g = scan.adjoint(pts, w, precision=_abi.FP32C)
+
+    def loss():
+        s = Scan(desc, device=0)
+        p, _ = s.run(_abi.FP64)
+        s.close()
+        return float((w * p["force"][:, 2]).sum())
+
+    fd_check(g, pert, loss)

@@ -287,3 +287,27 @@ def test_grid_rebuild_is_identical_and_captures_with_the_plan():
     # a scan without a rigid grid: no-op
     other = Scan(Input(golden("graphene_ef").input).desc(), device=0)
     _abi.check(L.mafm_scan_build_grid(other.handle, _abi.FP32C, None))
+
+
+def test_pinned_host_outputs_equal_device_outputs():
+    """Pinned host outputs (written by the kernel directly) hold the same bits
+    as pageable host outputs (staged) for mafm_run and mafm_run_batch."""
+    import torch
+    names = ["graphene_euler", "cluster_f"]
+    scans = [Scan(Input(golden(n).input).desc(), device=0) for n in names]
+    for prec in (_abi.FP64, _abi.FP32C):
+        want, _ = scans[1].run(prec, lanes=2)
+        buf = torch.zeros(scans[1].desc.n_points * 64, dtype=torch.uint8, pin_memory=True)
+        got, _ = scans[1].run(prec, lanes=2, out=buf.numpy().view(_abi.POINT_DTYPE))
+        np.testing.assert_array_equal(got["tip"], want["tip"])
+        np.testing.assert_array_equal(got["steps"], want["steps"])
+    want, _ = run_batch(scans, lanes=2)
+    import ctypes as C
+    bufs = [torch.zeros(s.desc.n_points * 64, dtype=torch.uint8, pin_memory=True) for s in scans]
+    outs = (C.c_void_p * 2)(*[b.data_ptr() for b in bufs])
+    handles = (C.c_void_p * 2)(*[s.handle for s in scans])
+    st = _abi.RunStats()
+    o = _abi.RunOpts(_abi.FP32C, 2, 0, 0, 0, 0)
+    _abi.check(_abi.lib().mafm_run_batch(handles, 2, C.byref(o), outs, C.byref(st), None))
+    for b, w in zip(bufs, want):
+        np.testing.assert_array_equal(b.numpy().view(_abi.POINT_DTYPE)["tip"], w["tip"])
