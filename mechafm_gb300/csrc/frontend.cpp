@@ -793,6 +793,76 @@ void prepare(mafm_input& in) {
 
 namespace {
 
+// Longest "%W.Pf" of a double (309 integer digits, sign, point, decimals).
+constexpr int kFieldMax = 340;
+
+// printf("%W.Pf", x) for the writer's fields, without printf: glibc prints
+// the exact binary value rounded to P decimals (to nearest, ties to even),
+// so the value is taken apart (x = m 2^e, m < 2^53) and m 10^P 2^e is rounded
+// in 128-bit integer arithmetic.  A negative value that rounds to zero keeps
+// its sign ("-0.000"), as printf does.  Values that are not finite or not
+// below 1e12 in magnitude go to snprintf.
+char* put_fixed(char* o, double x, int width, int prec) {
+    static const uint64_t kPow10[] = {1, 10, 100, 1000, 10000, 100000, 1000000};
+    if (!(std::fabs(x) < 1e12) || prec > 6) return o + snprintf(o, kFieldMax, "%*.*f", width, prec, x);
+    uint64_t bits;
+    std::memcpy(&bits, &x, sizeof bits);
+    const bool neg = (bits >> 63) != 0;
+    const int bexp = (int)((bits >> 52) & 0x7ff);
+    uint64_t m = bits & ((1ull << 52) - 1);
+    int e;
+    if (bexp == 0) {
+        e = -1074;
+    } else {
+        m |= 1ull << 52;
+        e = bexp - 1075;
+    }
+    const unsigned __int128 N = (unsigned __int128)m * kPow10[prec];   // < 2^73
+    uint64_t q;
+    if (e >= 0) {
+        q = (uint64_t)(N << e);
+    } else if (-e >= 100) {
+        q = 0;   // m 10^P 2^e < 2^73 / 2^100: below one half
+    } else {
+        const int sh = -e;
+        unsigned __int128 qq = N >> sh;
+        const unsigned __int128 rem = N - (qq << sh);
+        const unsigned __int128 half = (unsigned __int128)1 << (sh - 1);
+        if (rem > half || (rem == half && (qq & 1))) ++qq;
+        q = (uint64_t)qq;
+    }
+    char dig[32];
+    int n = 0;
+    do {
+        dig[n++] = (char)('0' + q % 10);
+        q /= 10;
+    } while (q);
+    while (n <= prec) dig[n++] = '0';   // one integer digit at least
+    const int len = n + (prec > 0 ? 1 : 0) + (neg ? 1 : 0);
+    for (int s = len; s < width; ++s) *o++ = ' ';
+    if (neg) *o++ = '-';
+    for (int d = n - 1; d >= prec; --d) *o++ = dig[d];
+    if (prec > 0) {
+        *o++ = '.';
+        for (int d = prec - 1; d >= 0; --d) *o++ = dig[d];
+    }
+    return o;
+}
+
+// printf("%d", v)
+char* put_int(char* o, long long v) {
+    char dig[24];
+    int n = 0;
+    unsigned long long u = v < 0 ? 0ull - (unsigned long long)v : (unsigned long long)v;
+    do {
+        dig[n++] = (char)('0' + u % 10);
+        u /= 10;
+    } while (u);
+    if (v < 0) *o++ = '-';
+    while (n) *o++ = dig[--n];
+    return o;
+}
+
 void write_rows(const mafm_input& in, const mafm_point* pts, int k, FILE* f) {
     const int nx = in.np[0], ny = in.np[1], nz = in.np[2];
     // Dummy z after k calls of lowerTip (system.hpp:51-54).
@@ -802,7 +872,7 @@ void write_rows(const mafm_input& in, const mafm_point* pts, int k, FILE* f) {
     const M3 inv = in.cell.inverse();
     std::string buf;
     buf.reserve((size_t)ny * 120);
-    char row[512];
+    char row[16 * kFieldMax];
     for (int i = 0; i < nx; ++i) {
         buf.clear();
         for (int j = 0; j < ny; ++j) {
@@ -824,12 +894,21 @@ void write_rows(const mafm_input& in, const mafm_point* pts, int k, FILE* f) {
             const double rx = p.tip[0] - dxy[0], ry = p.tip[1] - dxy[1], rz = p.tip[2] - dz_acc;
             const double r = sqrt(rx * rx + ry * ry + rz * rz);
             const double angle = atan2(sqrt(rx * rx + ry * ry), rz) * (180.0 / kPi);
-            int len = snprintf(row, sizeof row,
-                               "%d %d %d %6.3f %6.3f %6.3f %8.4f %8.4f %8.4f %6.3f %6.3f %6.3f "
-                               "%6.3f %8.4f %8.4f %d\n",
-                               k, i, j, x, y, dz_acc, p.force[0], p.force[1], p.force[2], rx, ry,
-                               rz, r, angle, p.energy, p.steps);
-            buf.append(row, (size_t)len);
+            // "%d %d %d %6.3f %6.3f %6.3f %8.4f %8.4f %8.4f %6.3f %6.3f %6.3f %6.3f %8.4f %8.4f %d\n"
+            char* o = row;
+            o = put_int(o, k); *o++ = ' ';
+            o = put_int(o, i); *o++ = ' ';
+            o = put_int(o, j); *o++ = ' ';
+            const double f3[3] = {x, y, dz_acc};
+            for (double v : f3) { o = put_fixed(o, v, 6, 3); *o++ = ' '; }
+            for (int c = 0; c < 3; ++c) { o = put_fixed(o, p.force[c], 8, 4); *o++ = ' '; }
+            const double g4[4] = {rx, ry, rz, r};
+            for (double v : g4) { o = put_fixed(o, v, 6, 3); *o++ = ' '; }
+            o = put_fixed(o, angle, 8, 4); *o++ = ' ';
+            o = put_fixed(o, p.energy, 8, 4); *o++ = ' ';
+            o = put_int(o, p.steps);
+            *o++ = '\n';
+            buf.append(row, (size_t)(o - row));
         }
         fwrite(buf.data(), 1, buf.size(), f);
     }
