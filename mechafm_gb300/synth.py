@@ -259,8 +259,12 @@ def slab(seed: int = 7, nlx: int = 16, nly: int = 32, layers: int = 4,
          cell=(40.0, 40.0, 30.0), cube_n=(160, 160, 120), pixels: int = 512,
          step: float = 0.2, zhigh: float = 16.0, zlow: float = 12.0, dz: float = 0.1,
          rigidgrid: bool = True, external: bool = True, tip_charge: float = -0.1,
-         **opt) -> ScanInput:
-    """Periodic slab (layers of nlx x nly sites), vdw_pbc, optional cube and grid."""
+         shear: float = 0.0, **opt) -> ScanInput:
+    """Periodic slab (layers of nlx x nly sites), vdw_pbc, optional cube and grid.
+
+    shear tilts the cell's b vector to (shear b, b, 0): the atoms keep their
+    fractional coordinates and the cube its values, on sheared voxels (a
+    non-orthogonal cube basis)."""
     rng = np.random.default_rng(seed)
     a, b, c = cell
     xs = (np.arange(nlx) + 0.5) * (a / nlx)
@@ -271,7 +275,9 @@ def slab(seed: int = 7, nlx: int = 16, nly: int = 32, layers: int = 4,
             for j, y in enumerate(ys):
                 pos.append((x, y, 10.0 + 2.0 * L))
                 types.append("C" if (i + j + L) % 2 == 0 else "N")
-    pos = np.array(pos)
+    frac_pos = np.array(pos)                 # orthorhombic frame (fractional x cell)
+    pos = frac_pos.copy()
+    pos[:, 0] += shear * pos[:, 1]           # (shear b, b, 0) for the b vector
     q = rng.normal(0.0, 0.3, size=len(pos))
     params = {"C": (0.086, 3.4, 12.011, 0.0), "N": (0.17, 3.25, 14.007, 0.0),
               TIP[0]: (TIP[1], TIP[2], 15.999, tip_charge), DUMMY[0]: (DUMMY[1], DUMMY[2], 0.0, 0.0)}
@@ -279,12 +285,13 @@ def slab(seed: int = 7, nlx: int = 16, nly: int = 32, layers: int = 4,
     o = base_options(area=f"{area!r} {area!r}", dx=step, dy=step, zhigh=zhigh, zlow=zlow,
                      dz=dz, vdw_pbc="on", rigidgrid="on" if rigidgrid else "off")
     if not external:
-        o.update(cell_a=f"{a} 0 0", cell_b=f"0 {b} 0", cell_c=f"0 0 {c}")
+        o.update(cell_a=f"{a} 0 0", cell_b=f"{_fmt(shear * b)} {b} 0", cell_c=f"0 0 {c}")
     cube = None
     if external:
         o["use_external_potential"] = "on"
         voxel = np.diag([a / cube_n[0], b / cube_n[1], c / cube_n[2]])
-        v = gaussian_potential(pos, q, np.diag(cell), cube_n)
+        voxel[1, 0] = shear * b / cube_n[1]
+        v = gaussian_potential(frac_pos, q, np.diag(cell), cube_n)
         cube = {"values": v, "voxel": voxel, "origin": (0.0, 0.0, 0.0)}
     o.update({k: str(v) for k, v in opt.items()})
     return ScanInput("slab", types, pos, None, params, [], (0.5, 0.0), o, cube)

@@ -41,11 +41,13 @@ def _vec(v):
     return " ".join(repr(float(x)) for x in v)
 
 
-def small_slab(rigidgrid: bool, voxels: int = 24):
-    """36-atom periodic slab, 6x6x10 A cell; 24 voxels = 0.25 A as the full-size slab."""
+def small_slab(rigidgrid: bool, voxels: int = 24, shear: float = 0.0, zlow: float = 9.0):
+    """36-atom periodic slab, 6x6x10 A cell; 24 voxels = 0.25 A as the full-size slab.
+    shear tilts the cell (a non-orthogonal cube basis)."""
     return synth.slab(seed=3, nlx=3, nly=6, layers=2, cell=(6.0, 6.0, 10.0),
-                      cube_n=(voxels, voxels, voxels * 10 // 6), pixels=5, step=0.5, zhigh=10.0,
-                      zlow=9.0, dz=0.1, rigidgrid=rigidgrid, external=True)
+                      cube_n=(voxels, voxels, voxels * 10 // 6), pixels=5, step=0.5,
+                      zhigh=zlow + 1.0, zlow=zlow, dz=0.1, rigidgrid=rigidgrid, external=True,
+                      shear=shear)
 
 
 def cases():
@@ -72,6 +74,10 @@ def cases():
     # 0.5 A voxels under-resolve the 0.5 A tip Gaussian: the reference stops with
     # "Imaginary part of inverse FFT exceeded threshold" (fft.cpp:79-83).
     c.append(("slab_es_coarse", small_slab(False, voxels=12), None, "error"))
+    # non-orthogonal cube basis: b tilted by 30 % of its length (with a rigid
+    # grid on top the reference stops: the tip leaves the grid at every shear
+    # and height tried, so only the pair + field form is a fixture)
+    c.append(("slab_es_tric", small_slab(False, shear=0.3), (0, 5, 0, 5), "sample_es"))
     c.append(("cluster_tdcoul_ev", synth.cluster_60(zlow=8.0, units="eV",
                                                     tip_dummy_coulomb="on"),
               (200, 203, 200, 203), None))
@@ -128,12 +134,19 @@ def make_cli_fixture(name, spec):
     return {"input": os.path.basename(inp), "cli": True, "rows": len(rows)}
 
 
-def main():
+def main(only=()):
+    """Regenerate every fixture, or only the named cases (the manifest keeps the others)."""
     oracle.build()
     if not oracle.ref_available():
         raise SystemExit("reference build missing")
     manifest = {}
+    mpath = os.path.join(HERE, "manifest.json")
+    if only and os.path.exists(mpath):
+        with open(mpath) as f:
+            manifest = json.load(f)
     for name, spec, block, sample in cases():
+        if only and name not in only:
+            continue
         folder = os.path.join(HERE, name)
         if os.path.isdir(folder):
             shutil.rmtree(folder)
@@ -179,6 +192,8 @@ def main():
                           "points": int(len(rec)), "sample": sample}
         print(name, len(rec), "points, mean steps", rec[:, 3].mean())
     for name, spec in cli_cases():
+        if only and name not in only:
+            continue
         manifest[name] = make_cli_fixture(name, spec)
         print(name, manifest[name]["rows"], "rows from the reference executable")
     with open(os.path.join(HERE, "manifest.json"), "w") as f:
@@ -186,4 +201,4 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    main(tuple(sys.argv[1:]))

@@ -13,7 +13,7 @@ import oracle
 from conftest import ERROR_CASES, POINT_CASES, golden
 from mechafm_gb300.scan import Input
 
-FFT_CASES = {"slab_es", "slab_es_grid"}
+FFT_CASES = {"slab_es", "slab_es_grid", "slab_es_tric"}
 
 
 def run_block(case):
