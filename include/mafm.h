@@ -111,7 +111,8 @@ typedef struct mafm_scan_desc {
     double offset[3];           /* System offset of the centring / z shift */
     /* scan geometry (mechafm.cpp:47-49, simulation.cpp:78-122) */
     int32_t nx, ny, nz;
-    int32_t reserved0;
+    int32_t flexible;           /* 1: the surface atoms move (flexible on); such a
+                                   scan runs through mafm_flex_* with its topology */
     double dx, dy, dz;
     double zhigh, zlow;
     double area[2];
@@ -177,6 +178,53 @@ int mafm_abi_version(void);
 int mafm_input_load(const char* input_file, int verbose, mafm_input** out);
 /* Fill a descriptor whose pointers refer to storage owned by `in`. */
 int mafm_input_desc(const mafm_input* in, mafm_scan_desc* out);
+
+/* ---- flexible molecules ------------------------------------------------------
+ * With `flexible on` every surface atom whose xyz "fixed" column is not 1
+ * moves (parse.cpp:559-563), held by the topology Simulation::
+ * buildSurfaceSurfaceInteractions and buildSubstrateInteractions build
+ * (simulation.cpp:516-693): harmonic bonds between atoms closer than 1.1 r0
+ * of a `topobond`, angles between bonds sharing an atom, dihedrals between
+ * angles, van der Waals (+ Coulomb) pairs between atoms not connected by
+ * bonds, a substrate wall on every atom and an XY tether on atoms with
+ * fixed = 2.  Atom indices below are surface-atom indices (0-based, the
+ * reference's System index - 2); every list is in the reference's
+ * interaction order, which is the order forces are summed per atom. */
+typedef struct mafm_flex_desc {
+    const int32_t* fixed;           /* [n_atoms] 0 free, 1 fixed, 2 XY-tethered */
+    int32_t n_bonds;                /* HarmonicInteraction (interactions.cpp:298-309) */
+    const int32_t* bond_atoms;      /* [n_bonds*2] i, j */
+    const double* bond_param;       /* [n_bonds*2] k, r0 */
+    int32_t n_angles;               /* HarmonicAngleInteraction (:311-338) */
+    const int32_t* angle_atoms;     /* [n_angles*3] shared, atom1, atom2 */
+    const double* angle_param;      /* [n_angles*2] k, theta0 */
+    int32_t n_dihedrals;            /* HarmonicDihedralInteraction (:340-370) */
+    const int32_t* dihedral_atoms;  /* [n_dihedrals*4] atom1..atom4 */
+    const double* dihedral_param;   /* [n_dihedrals*2] k, sigma0 */
+    int32_t n_pairs;                /* non-bonded surface pairs (simulation.cpp:678-690) */
+    const int32_t* pair_atoms;      /* [n_pairs*2] i < j */
+    const mafm_pair* pair_vdw;      /* [n_pairs] LJ / Morse */
+    const double* pair_qq;          /* [n_pairs] qbase q_i q_j, 0 = no Coulomb term */
+    double substrate[5];            /* eps, sig, lambda, rc, k (parse.cpp:741-747) */
+} mafm_flex_desc;
+
+/* The flexible topology of a `flexible on` input (storage owned by `in`). */
+int mafm_input_flex_desc(const mafm_input* in, mafm_flex_desc* out);
+
+/* A device-resident flexible scan: one warp relaxes every atom of a pixel
+ * column in FP64, each atom's force summed in the reference's interaction
+ * order.  Pair and Coulomb terms only (no rigid grid, no external field:
+ * the reference refuses both with flexible molecules, parse.cpp:387-395). */
+typedef struct mafm_flex mafm_flex;
+int mafm_flex_create(int device, const mafm_scan_desc* desc, const mafm_flex_desc* flex,
+                     mafm_flex** out);
+int mafm_flex_destroy(mafm_flex* flex);
+/* Relax columns [col_begin, col_end) (0, 0 = all); out as for mafm_run.
+ * states != NULL receives, for column state_column, every atom's position
+ * after each height: [nz][n_atoms + 2][3] (dummy, tip, surface atoms), what
+ * System::makeXYZFile writes for the middle pixel (simulation.cpp:114-116). */
+int mafm_flex_run(mafm_flex* flex, int32_t col_begin, int32_t col_end, mafm_point* out,
+                  mafm_run_stats* stats, int32_t state_column, double* states, void* stream);
 /* Output options of the input file: gzip, statistics, bufsize. */
 int mafm_input_output_opts(const mafm_input* in, int32_t* gzip, int32_t* statistics,
                            int32_t* bufsize);
@@ -336,6 +384,13 @@ int mafm_scan_build_grid(mafm_scan* scan, int32_t precision, void* stream);
  * must end in '/' otherwise.  Rows are written in point order. */
 int mafm_write_output(const mafm_input* in, const mafm_point* pts, const char* folder,
                       int32_t gzip);
+/* System::makeXYZFile (system.cpp:54-66) for every height of one column of
+ * a flexible scan: writes <folder>state_<x>-<y>-<z>.xyz (%.1f each: the pixel
+ * position and the dummy height) with every atom's type and position, and
+ * prints the reference's "+- Wrote <file>" line.  states as filled by
+ * mafm_flex_run: [nz][n_atoms + 2][3]. */
+int mafm_write_states(const mafm_input* in, const double* states, int32_t column,
+                      const char* folder);
 /* statistics.txt of finalize (mechafm.cpp:140-152). */
 int mafm_write_statistics(const mafm_input* in, const char* folder, uint64_t total_steps,
                           double wall_s, double total_s);

@@ -42,7 +42,7 @@ class ScanDesc(C.Structure):
         ("harm_k", C.c_double), ("harm_r0", C.c_double), ("tip_dummy_d", C.c_double),
         ("vdw_pbc", C.c_int32), ("tip_pbc", C.c_int32),
         ("cell", C.c_double * 9), ("offset", C.c_double * 3),
-        ("nx", C.c_int32), ("ny", C.c_int32), ("nz", C.c_int32), ("reserved0", C.c_int32),
+        ("nx", C.c_int32), ("ny", C.c_int32), ("nz", C.c_int32), ("flexible", C.c_int32),
         ("dx", C.c_double), ("dy", C.c_double), ("dz", C.c_double),
         ("zhigh", C.c_double), ("zlow", C.c_double), ("area", C.c_double * 2),
         ("minimiser", C.c_int32), ("integrator", C.c_int32),
@@ -75,6 +75,21 @@ class RunStats(C.Structure):
     _fields_ = [("total_steps", C.c_uint64), ("force_evals", C.c_uint64),
                 ("pair_evals", C.c_uint64), ("error_word", C.c_uint32),
                 ("reserved", C.c_uint32), ("kernel_ms", C.c_double)]
+
+
+class FlexDesc(C.Structure):
+    _fields_ = [
+        ("fixed", C.POINTER(C.c_int32)),
+        ("n_bonds", C.c_int32), ("bond_atoms", C.POINTER(C.c_int32)),
+        ("bond_param", C.POINTER(C.c_double)),
+        ("n_angles", C.c_int32), ("angle_atoms", C.POINTER(C.c_int32)),
+        ("angle_param", C.POINTER(C.c_double)),
+        ("n_dihedrals", C.c_int32), ("dihedral_atoms", C.POINTER(C.c_int32)),
+        ("dihedral_param", C.POINTER(C.c_double)),
+        ("n_pairs", C.c_int32), ("pair_atoms", C.POINTER(C.c_int32)),
+        ("pair_vdw", C.POINTER(Pair)), ("pair_qq", C.POINTER(C.c_double)),
+        ("substrate", C.c_double * 5),
+    ]
 
 
 class DfParams(C.Structure):
@@ -114,6 +129,13 @@ SIGNATURES = {
                                 C.POINTER(C.c_double), _P]),
     "mafm_adjoint": (C.c_int, [_P, _P, _P, C.POINTER(Grad), _P]),
     "mafm_adjoint_ex": (C.c_int, [_P, C.c_int32, _P, _P, C.POINTER(Grad), _P]),
+    "mafm_input_flex_desc": (C.c_int, [_P, C.POINTER(FlexDesc)]),
+    "mafm_write_states": (C.c_int, [_P, _P, C.c_int32, C.c_char_p]),
+    "mafm_flex_create": (C.c_int, [C.c_int, C.POINTER(ScanDesc), C.POINTER(FlexDesc),
+                                   C.POINTER(C.c_void_p)]),
+    "mafm_flex_destroy": (C.c_int, [_P]),
+    "mafm_flex_run": (C.c_int, [_P, C.c_int32, C.c_int32, _P, C.POINTER(RunStats), C.c_int32,
+                                _P, _P]),
     "mafm_df_weights": (C.c_int, [C.POINTER(DfParams), C.c_double, _P, C.c_int32,
                                   C.POINTER(C.c_int32), C.POINTER(C.c_double)]),
     "mafm_df": (C.c_int, [_P, C.c_int64, C.c_int32, C.c_int32, C.c_int32, C.c_double,

@@ -55,6 +55,7 @@ def _units():
         ([nv] + common + [os.path.join(CSRC, "noalloc.cu")], "noalloc.o"),
         ([nv] + common + [os.path.join(CSRC, "adjoint.cu")], "adjoint.o"),
         ([nv] + common + [os.path.join(CSRC, "df.cu")], "df.o"),
+        ([nv] + common + ["-fmad=false", os.path.join(CSRC, "flex.cu")], "flex.o"),
         (["g++", "-O2", "-fPIC", "-fopenmp", "-ffp-contract=off", "-std=c++17", "-Wall",
           "-I" + INCLUDE, "-I" + cuda_inc, "-c", os.path.join(CSRC, "frontend.cpp")],
          "frontend.o"),

@@ -14,8 +14,11 @@
 // Everything here is compiled with -ffp-contract=off: the reference is built
 // for x86-64 without FMA, and the host arithmetic (centring, mixing, matrix
 // inverse) must give the same bits on an aarch64 host.
+#include <algorithm>
+#include <array>
 #include <cctype>
 #include <cmath>
+#include <functional>
 #include <cstdarg>
 #include <cstdio>
 #include <cstdlib>
@@ -162,6 +165,11 @@ struct mafm_input {
     double harm_k = 0, harm_r0 = 0;
     double bond_k = 0, angle_k = 0, dihedral_k = 0;
     double sub_eps = 0, sub_sig = 0, sub_lambda = 0, sub_rc = 0, sub_k = 0;
+    struct TopoBond {
+        std::string a, b;
+        double r0;
+    };
+    std::vector<TopoBond> topobonds;   // possible_bonds_ (parse.cpp:748-765)
     std::map<std::string, mafm::AtomParams> ap;
     std::vector<mafm::Overwrite> ow;
     // --- System (system.hpp:13-77); index 0 dummy, 1 tip, 2.. surface ---
@@ -178,6 +186,10 @@ struct mafm_input {
     // --- descriptor storage ---
     std::vector<double> d_pos, d_charge;
     std::vector<int32_t> d_type;
+    // flexible topology (surface-atom indices), mafm_flex_desc storage
+    std::vector<int32_t> f_fixed, f_bond_atoms, f_angle_atoms, f_dihedral_atoms, f_pair_atoms;
+    std::vector<double> f_bond_param, f_angle_param, f_dihedral_param, f_pair_qq;
+    std::vector<mafm_pair> f_pair_vdw;
     std::vector<mafm_pair> d_pairs;
     std::vector<std::string> type_names;
     mafm_pair dummy_pair{};
@@ -451,8 +463,7 @@ void read_xyz(mafm_input& in) {
     }
 }
 
-// readFlexibleParameters, parse.cpp:699-782 (parsed for completeness of the
-// boundary; flexible scans are not run on the GPU).
+// readFlexibleParameters, parse.cpp:699-782.
 void read_flexible(mafm_input& in, FILE* fp) {
     char line[kLine], keyword[128] = "", dump[128];
     bool b = false, a = false, d = false, s = false;
@@ -479,6 +490,16 @@ void read_flexible(mafm_input& in, FILE* fp) {
             sscanf(line, "%127s %lf %lf %lf %lf %lf", dump, &in.sub_eps, &in.sub_sig,
                    &in.sub_lambda, &in.sub_rc, &in.sub_k);
             s = true;
+        }
+        if (!strcmp(keyword, "topobond")) {
+            char a1[128] = "", a2[128] = "";
+            double r0 = 0;
+            sscanf(line, "%127s %127s %127s %lf", dump, a1, a2, &r0);
+            bool twice = false;
+            for (const auto& tb : in.topobonds)
+                if (multiset_eq(tb.a, tb.b, a1, a2)) twice = true;
+            if (twice) warn(in, "The topobond for %s and %s is defined at least twice!", a1, a2);
+            in.topobonds.push_back({a1, a2, r0});
         }
     }
     if (!b) fail(MAFM_E_PARSE, "No harmonic bond parameters found in parameter file!");
@@ -663,6 +684,123 @@ double coulomb_charge(const mafm_input& in, int i) {
     return it->second.q;
 }
 
+// Simulation::buildSurfaceSurfaceInteractions (simulation.cpp:557-693) for a
+// flexible molecule, with the reference's vector arithmetic (vectors.hpp:99-125):
+// bonds between atoms closer than 1.1 r0 of a topobond (r0 of the spring = the
+// distance), angles between bonds sharing an atom, dihedrals between angles
+// (the reference's five patterns, each improper centre once), and van der
+// Waals (+ Coulomb) pairs between atoms of different bonded fragments.
+// "Connected" is the reference's breadth-first search to a depth of the atom
+// count, i.e. the same bonded fragment.  Indices stored are surface indices.
+void build_topology(mafm_input& in) {
+    const int n = in.n_atoms;
+    auto sub = [&](int a, int b, double r[3]) {
+        for (int d = 0; d < 3; ++d) r[d] = in.pos[3 * (size_t)a + d] - in.pos[3 * (size_t)b + d];
+    };
+    auto len = [](const double r[3]) { return sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]); };
+    auto dot = [](const double a[3], const double b[3]) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; };
+    auto cross = [](const double a[3], const double b[3], double r[3]) {
+        r[0] = a[1] * b[2] - a[2] * b[1];
+        r[1] = a[2] * b[0] - a[0] * b[2];
+        r[2] = a[0] * b[1] - a[1] * b[0];
+    };
+    auto normalized = [&](const double a[3], double r[3]) {
+        const double l = len(a);
+        for (int d = 0; d < 3; ++d) r[d] = l > 1e-10 ? a[d] / l : 0.0;
+    };
+    in.f_fixed.assign(in.fixed.begin() + 2, in.fixed.end());
+    in.f_bond_atoms.clear(); in.f_bond_param.clear();
+    in.f_angle_atoms.clear(); in.f_angle_param.clear();
+    in.f_dihedral_atoms.clear(); in.f_dihedral_param.clear();
+    in.f_pair_atoms.clear(); in.f_pair_vdw.clear(); in.f_pair_qq.clear();
+    // bonds, and the bonded fragments (union-find)
+    std::vector<int> root(n);
+    for (int i = 0; i < n; ++i) root[i] = i;
+    std::function<int(int)> find = [&](int x) { return root[x] == x ? x : (root[x] = find(root[x])); };
+    std::vector<std::pair<int, int>> bonds;
+    for (int i = 2; i < n; ++i)
+        for (int j = i + 1; j < n; ++j) {
+            double r0 = 0;
+            for (const auto& tb : in.topobonds)
+                if (multiset_eq(tb.a, tb.b, in.types[i], in.types[j])) r0 = tb.r0;
+            double r[3];
+            sub(i, j, r);
+            const double atom_d = len(r);
+            if (atom_d < 1.1 * r0) {
+                bonds.emplace_back(i, j);
+                root[find(i)] = find(j);
+                in.f_bond_atoms.insert(in.f_bond_atoms.end(), {i - 2, j - 2});
+                in.f_bond_param.insert(in.f_bond_param.end(), {in.bond_k, atom_d});
+            }
+        }
+    // angles
+    std::vector<std::array<int, 3>> angles;
+    for (size_t bi = 0; bi < bonds.size(); ++bi)
+        for (size_t bj = bi + 1; bj < bonds.size(); ++bj) {
+            const auto b1 = bonds[bi], b2 = bonds[bj];
+            int shared = -1, a1 = 0, a2 = 0;
+            if (b1.first == b2.first) { shared = b1.first; a1 = b1.second; a2 = b2.second; }
+            else if (b1.first == b2.second) { shared = b1.first; a1 = b1.second; a2 = b2.first; }
+            else if (b1.second == b2.first) { shared = b1.second; a1 = b1.first; a2 = b2.second; }
+            else if (b1.second == b2.second) { shared = b1.second; a1 = b1.first; a2 = b2.first; }
+            if (shared == -1) continue;
+            angles.push_back({shared, a1, a2});
+            double d1[3], d2[3], n1[3], n2[3];
+            sub(a1, shared, d1);
+            sub(a2, shared, d2);
+            normalized(d1, n1);
+            normalized(d2, n2);
+            const double theta0 = acos(dot(n1, n2));
+            in.f_angle_atoms.insert(in.f_angle_atoms.end(), {shared - 2, a1 - 2, a2 - 2});
+            in.f_angle_param.insert(in.f_angle_param.end(), {in.angle_k, theta0});
+        }
+    // dihedrals
+    std::vector<int> improper;
+    for (size_t ai = 0; ai < angles.size(); ++ai)
+        for (size_t aj = ai + 1; aj < angles.size(); ++aj) {
+            const auto& g1 = angles[ai];
+            const auto& g2 = angles[aj];
+            int t1 = -1, t2 = -1, t3 = -1, t4 = -1;
+            if (g1[0] == g2[0] && std::find(improper.begin(), improper.end(), g1[0]) == improper.end()) {
+                improper.push_back(g1[0]);
+                t1 = g1[0]; t2 = g1[1]; t3 = g1[2];
+                t4 = (g2[1] == g1[1] || g2[1] == g1[2]) ? g2[2] : g2[1];
+            } else if (g1[1] == g2[0] && g2[1] == g1[0]) {
+                t1 = g1[2]; t2 = g1[0]; t3 = g2[0]; t4 = g2[2];
+            } else if (g1[2] == g2[0] && g2[1] == g1[0]) {
+                t1 = g1[1]; t2 = g1[0]; t3 = g2[0]; t4 = g2[2];
+            } else if (g1[1] == g2[0] && g2[2] == g1[0]) {
+                t1 = g1[2]; t2 = g1[0]; t3 = g2[0]; t4 = g2[1];
+            } else if (g1[2] == g2[0] && g2[2] == g1[0]) {
+                t1 = g1[1]; t2 = g1[0]; t3 = g2[0]; t4 = g2[1];
+            }
+            if (t1 == -1) continue;
+            double d12[3], d23[3], d43[3], m[3], nn[3];
+            sub(t1, t2, d12);
+            sub(t2, t3, d23);
+            sub(t4, t3, d43);
+            cross(d12, d23, m);
+            cross(d43, d23, nn);
+            const double tan_s = dot(nn, d12) * len(d23) / (dot(m, nn));
+            const double sigma0 = atan(tan_s);
+            in.f_dihedral_atoms.insert(in.f_dihedral_atoms.end(), {t1 - 2, t2 - 2, t3 - 2, t4 - 2});
+            in.f_dihedral_param.insert(in.f_dihedral_param.end(), {in.dihedral_k, sigma0});
+        }
+    // non-bonded pairs between fragments: addVDWInteraction, addCoulombInteraction
+    for (int i = 2; i < n; ++i)
+        for (int j = i + 1; j < n; ++j) {
+            if (find(i) == find(j)) continue;
+            in.f_pair_atoms.insert(in.f_pair_atoms.end(), {i - 2, j - 2});
+            in.f_pair_vdw.push_back(resolve_vdw(in, in.types[i], in.types[j]));
+            double qq = 0;
+            if (in.coulomb) {
+                const double q1 = coulomb_charge(in, i), q2 = coulomb_charge(in, j);
+                if (q1 != 0 && q2 != 0) qq = in.qbase * q1 * q2;
+            }
+            in.f_pair_qq.push_back(qq);
+        }
+}
+
 // Simulation::initialize and the parameter part of buildInteractions.
 void prepare(mafm_input& in) {
     in.np[0] = (int)(floor(in.area[0] / in.dx) + 1);
@@ -785,6 +923,7 @@ void prepare(mafm_input& in) {
         in.epot_basis = basis;
         in.epot.swap(c.values);
     }
+    if (in.flexible) build_topology(in);
 }
 
 }  // namespace
@@ -950,9 +1089,8 @@ int mafm_input_load(const char* input_file, int verbose, mafm_input** out) {
 int mafm_input_desc(const mafm_input* in, mafm_scan_desc* d) {
     return mafm::guarded([&] {
         if (!in || !d) mafm::fail(MAFM_E_INVALID, "null argument");
-        if (in->flexible)
-            mafm::fail(MAFM_E_UNSUPPORTED, "flexible molecules are not run by this library");
         *d = mafm_scan_desc{};
+        d->flexible = in->flexible;
         d->n_atoms = in->n_atoms - 2;
         d->n_types = (int32_t)in->type_names.size();
         d->pos = in->d_pos.data();
@@ -1002,6 +1140,33 @@ int mafm_input_desc(const mafm_input* in, mafm_scan_desc* d) {
     });
 }
 
+int mafm_input_flex_desc(const mafm_input* in, mafm_flex_desc* f) {
+    return mafm::guarded([&] {
+        if (!in || !f) mafm::fail(MAFM_E_INVALID, "null argument");
+        if (!in->flexible) mafm::fail(MAFM_E_INVALID, "the input is not a flexible molecule");
+        *f = mafm_flex_desc{};
+        f->fixed = in->f_fixed.data();
+        f->n_bonds = (int32_t)in->f_bond_param.size() / 2;
+        f->bond_atoms = in->f_bond_atoms.data();
+        f->bond_param = in->f_bond_param.data();
+        f->n_angles = (int32_t)in->f_angle_param.size() / 2;
+        f->angle_atoms = in->f_angle_atoms.data();
+        f->angle_param = in->f_angle_param.data();
+        f->n_dihedrals = (int32_t)in->f_dihedral_param.size() / 2;
+        f->dihedral_atoms = in->f_dihedral_atoms.data();
+        f->dihedral_param = in->f_dihedral_param.data();
+        f->n_pairs = (int32_t)in->f_pair_qq.size();
+        f->pair_atoms = in->f_pair_atoms.data();
+        f->pair_vdw = in->f_pair_vdw.data();
+        f->pair_qq = in->f_pair_qq.data();
+        f->substrate[0] = in->sub_eps;
+        f->substrate[1] = in->sub_sig;
+        f->substrate[2] = in->sub_lambda;
+        f->substrate[3] = in->sub_rc;
+        f->substrate[4] = in->sub_k;
+    });
+}
+
 int mafm_input_output_opts(const mafm_input* in, int32_t* gzip, int32_t* statistics,
                            int32_t* bufsize) {
     return mafm::guarded([&] {
@@ -1041,6 +1206,31 @@ int mafm_write_output(const mafm_input* in, const mafm_point* pts, const char* f
         for (int k = 0; k < nz; ++k) {
             if (gzip) pclose(files[k]);
             else fclose(files[k]);
+        }
+    });
+}
+
+int mafm_write_states(const mafm_input* in, const double* states, int32_t column,
+                      const char* folder) {
+    return mafm::guarded([&] {
+        if (!in || !states || !folder) mafm::fail(MAFM_E_INVALID, "null argument");
+        const int nx = in->np[0], ny = in->np[1], nz = in->np[2], na = in->n_atoms;
+        if (column < 0 || column >= nx * ny) mafm::fail(MAFM_E_INVALID, "column %d outside the scan", column);
+        const double x = (column / ny) * in->dx, y = (column % ny) * in->dy;
+        double z = in->zhigh;
+        for (int k = 0; k < nz; ++k) {
+            char name[1024];
+            snprintf(name, sizeof name, "%sstate_%.1f-%.1f-%.1f.xyz", folder, x, y, z);
+            FILE* fp = fopen(name, "w");
+            if (!fp) mafm::fail(MAFM_E_IO, "cannot open %s", name);
+            fprintf(fp, "%d\n\n", na);
+            for (int a = 0; a < na; ++a) {
+                const double* p = states + ((size_t)k * na + a) * 3;
+                fprintf(fp, "%s %8.4f %8.4f %8.4f\n", in->types[a].c_str(), p[0], p[1], p[2]);
+            }
+            fclose(fp);
+            printf("+- Wrote %s\n", name);
+            z -= in->dz;
         }
     });
 }

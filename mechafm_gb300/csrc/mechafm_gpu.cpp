@@ -5,8 +5,9 @@
 // echo, error messages and exit status, scan-%06.3f.dat[.gz] files and
 // statistics.txt.  The relaxation runs through libmafm's C ABI.  By default it
 // runs the FP64 kernel, whose results are those of the reference; setting
-// MAFM_PRECISION=fp32c selects the FP32-compensated kernel.  MAFM_DEVICE picks
-// the GPU (default 0).
+// MAFM_PRECISION=fp32c selects the FP32-compensated kernel.  A flexible
+// molecule runs the FP64 flexible kernel and writes the middle pixel's
+// state_*.xyz files like the reference.  MAFM_DEVICE picks the GPU (default 0).
 #include <chrono>
 #include <cstdarg>
 #include <cstdio>
@@ -79,7 +80,15 @@ int main(int argc, char* argv[]) {
     if (d.use_external_potential)
         pretty("Calculating energy and force on grid from external electrostatic potential.");
     mafm_scan* scan = nullptr;
-    check(mafm_scan_create(device, &d, &scan));
+    mafm_flex* flex = nullptr;
+    if (d.flexible) {
+        // flexible molecule: every atom relaxes (FP64 flexible kernel)
+        mafm_flex_desc fd;
+        check(mafm_input_flex_desc(in, &fd));
+        check(mafm_flex_create(device, &d, &fd, &flex));
+    } else {
+        check(mafm_scan_create(device, &d, &scan));
+    }
     if (d.use_external_potential) pretty("Done!");
     if (d.rigidgrid) {
         int32_t n[3];
@@ -96,20 +105,32 @@ int main(int argc, char* argv[]) {
     std::vector<mafm_point> pts((size_t)n_total);
     uint64_t total_steps = 0;
     const int chunks = 10;
+    // flexible molecules: the middle pixel's states (simulation.cpp:114-116)
+    const int state_col = (d.nx * d.ny) / 2;
+    std::vector<double> states(d.flexible ? (size_t)d.nz * (d.n_atoms + 2) * 3 : 0);
     for (int c = 0; c < chunks; ++c) {
         const int i0 = (int)((long long)d.nx * c / chunks), i1 = (int)((long long)d.nx * (c + 1) / chunks);
         if (i1 <= i0) continue;
-        mafm_run_opts o{};
-        o.precision = precision;
-        o.col_begin = i0 * d.ny;
-        o.col_end = i1 * d.ny;
+        const int cb = i0 * d.ny, ce = i1 * d.ny;
         mafm_run_stats st{};
-        check(mafm_run(scan, &o, pts.data() + (size_t)o.col_begin * d.nz, &st, nullptr));
+        if (flex) {
+            const bool with_states = state_col >= cb && state_col < ce;
+            check(mafm_flex_run(flex, cb, ce, pts.data() + (size_t)cb * d.nz, &st, state_col,
+                                with_states ? states.data() : nullptr, nullptr));
+            if (with_states) check(mafm_write_states(in, states.data(), state_col, outdir.c_str()));
+        } else {
+            mafm_run_opts o{};
+            o.precision = precision;
+            o.col_begin = cb;
+            o.col_end = ce;
+            check(mafm_run(scan, &o, pts.data() + (size_t)cb * d.nz, &st, nullptr));
+        }
         total_steps += st.total_steps;
         pretty("Finished %4.1f %% of the simulation", 100.0 * i1 / d.nx);
     }
     check(mafm_write_output(in, pts.data(), outdir.c_str(), gzip));
-    check(mafm_scan_destroy(scan));
+    if (scan) check(mafm_scan_destroy(scan));
+    if (flex) check(mafm_flex_destroy(flex));
 
     // finalize (mechafm.cpp:103-154)
     const auto t_end = std::chrono::system_clock::now();

@@ -235,6 +235,7 @@ namespace {
 
 void validate(const mafm_scan_desc* d) {
     if (!d) fail(MAFM_E_INVALID, "null descriptor");
+    if (d->flexible) fail(MAFM_E_UNSUPPORTED, "a flexible molecule runs through mafm_flex_create");
     if (d->n_atoms < 0 || d->n_types < 0) fail(MAFM_E_INVALID, "negative atom or type count");
     if (d->n_atoms > 0 && (!d->pos || !d->type || !d->tip_pair))
         fail(MAFM_E_INVALID, "descriptor has atoms but null pos/type/tip_pair");

@@ -46,6 +46,12 @@ class Input:
         check(lib().mafm_input_desc(self._h, C.byref(d)))
         return Desc(d, keep=self)
 
+    def flex_desc(self) -> "FlexDesc":
+        """The flexible topology of a `flexible on` input (mafm_input_flex_desc)."""
+        f = _abi.FlexDesc()
+        check(lib().mafm_input_flex_desc(self._h, C.byref(f)))
+        return FlexDesc(f, keep=self)
+
     def output_opts(self):
         g, s, b = C.c_int32(), C.c_int32(), C.c_int32()
         check(lib().mafm_input_output_opts(self._h, C.byref(g), C.byref(s), C.byref(b)))
@@ -140,6 +146,48 @@ class Desc:
             "charge": np.ctypeslib.as_array(self.c.charge, shape=(n,)).copy(),
             "type": np.ctypeslib.as_array(self.c.type, shape=(n,)).copy(),
         }
+
+
+class FlexDesc:
+    """A mafm_flex_desc plus whatever owns the memory its pointers refer to."""
+
+    def __init__(self, c: _abi.FlexDesc, keep=None):
+        self.c = c
+        self._keep = keep
+
+
+class FlexScan:
+    """A device-resident flexible scan (mafm_flex): FP64, one warp per column."""
+
+    def __init__(self, desc: Desc, flex: FlexDesc, device: int = -1):
+        h = C.c_void_p()
+        check(lib().mafm_flex_create(device, C.byref(desc.c), C.byref(flex.c), C.byref(h)))
+        self._h = h
+        self.desc = desc
+        self.flex = flex
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().mafm_flex_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def run(self, col_begin=0, col_end=0, state_column=-1, stream=None):
+        """Relax columns [col_begin, col_end); returns (points, stats, states)
+        with states (nz, n_atoms + 2, 3) for state_column, or None."""
+        d = self.desc.c
+        n_cols = (col_end - col_begin) if col_end else d.nx * d.ny
+        out = np.zeros(n_cols * d.nz, dtype=_abi.POINT_DTYPE)
+        st = _abi.RunStats()
+        states = np.zeros((d.nz, d.n_atoms + 2, 3)) if state_column >= 0 else None
+        check(lib().mafm_flex_run(self._h, col_begin, col_end, ptr(out), C.byref(st), state_column,
+                                  ptr(states) if states is not None else None, stream))
+        return out, st, states
 
 
 def run_opts(precision=_abi.FP64, lanes=0, block=0, tile=0, col_begin=0, col_end=0):

@@ -87,6 +87,8 @@ class ScanInput:
                 f.write("pair_ovwrt " + " ".join(str(x) if isinstance(x, str) else _fmt(x)
                                                  for x in ow) + "\n")
             f.write(f"harm {_fmt(self.harm[0])} {_fmt(self.harm[1])}\n")
+            for line in getattr(self, "extra_param_lines", []):
+                f.write(line + "\n")
         opts = dict(self.options)
         opts["xyzfile"] = os.path.basename(xyz)
         opts["paramfile"] = os.path.basename(par)
@@ -199,6 +201,56 @@ def cluster_60(seed: int = 1234, area: float = 20.0, step: float = 0.05,
     o.update({k: str(v) for k, v in opt.items()})
     return ScanInput("cluster_60", types, pos, q, dict(CLUSTER_PARAMS),
                      [("O", "O", "morse", 0.1, 1.5, 3.2)], (0.5, 0.0), o)
+
+
+def naphthalene(cc: float = 1.40, ch: float = 1.09) -> tuple:
+    """C10H8 in the xy plane: two fused hexagons (C-C cc) with H at ch."""
+    carbons = []
+    for cx in (-cc * math.sqrt(3) / 2, cc * math.sqrt(3) / 2):
+        for k in range(6):
+            ang = math.radians(30 + 60 * k)
+            p = (cx + cc * math.cos(ang), cc * math.sin(ang))
+            if all(math.hypot(p[0] - q[0], p[1] - q[1]) > 0.1 for q in carbons):
+                carbons.append(p)
+    hydrogens = []
+    for p in carbons:
+        if abs(p[0]) < 1e-6:
+            continue                          # the two shared carbons carry no H
+        d = np.array(p) - np.array((math.copysign(cc * math.sqrt(3) / 2, p[0]), 0.0))
+        d /= np.linalg.norm(d)
+        hydrogens.append(tuple(np.array(p) + ch * d))
+    pos = [(x, y, 0.0) for x, y in carbons] + [(x, y, 0.0) for x, y in hydrogens]
+    return ["C"] * len(carbons) + ["H"] * len(hydrogens), np.array(pos)
+
+
+def flexible_naphthalene(seed: int = 21, area: float = 1.0, step: float = 0.5,
+                         zhigh: float = 10.0, zlow: float = 8.0, dz: float = 0.2,
+                         **opt) -> ScanInput:
+    """Flexible C10H8 and a separate H2, with charges: free atoms, two
+    XY-tethered hydrogens and one fixed carbon; bond / angle / dihedral /
+    substrate parameters and topobonds for C-C, C-H and H-H (parse.cpp:699-782)."""
+    rng = np.random.default_rng(seed)
+    types, pos = naphthalene()
+    # a separate H2 beside the ring: non-bonded pairs between the fragments
+    types = types + ["H", "H"]
+    pos = np.vstack([pos, [[4.6, -0.37, 0.3], [4.6, 0.37, 0.3]]])
+    pos = pos + rng.normal(0.0, 0.01, pos.shape) * np.array([1.0, 1.0, 0.0])
+    q = rng.normal(0.0, 0.1, len(types))
+    q -= q.mean()
+    fixed = np.zeros(len(types), dtype=int)
+    fixed[len(types) - 3] = 2
+    fixed[len(types) - 5] = 2
+    fixed[0] = 1
+    params = {"C": (0.086, 3.4, 12.011, 0.0), "H": (0.03, 2.5, 1.008, 0.0),
+              TIP[0]: (TIP[1], TIP[2], 15.999, -0.1), DUMMY[0]: (DUMMY[1], DUMMY[2], 0.0, 0.0)}
+    o = base_options(area=f"{area} {area}", dx=step, dy=step, zhigh=zhigh, zlow=zlow, dz=dz,
+                     coulomb="on", flexible="on")
+    o.update({k: str(v) for k, v in opt.items()})
+    spec = ScanInput("naph", types, pos, q, params, [], (0.5, 0.0), o, None, fixed)
+    spec.extra_param_lines = ["bond 50.0", "angle 20.0", "dihedral 2.0",
+                              "substrate 0.1 3.0 3.0 7.5 1.0",
+                              "topobond C C 1.40", "topobond C H 1.09", "topobond H H 0.74"]
+    return spec
 
 
 def write_cube(path: str, values: np.ndarray, voxel: np.ndarray, origin) -> None:

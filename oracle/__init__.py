@@ -44,6 +44,10 @@ def port():
         L.oracle_run_split.restype = C.c_int
         L.oracle_run_split.argtypes = [C.POINTER(_abi.ScanDesc), C.c_int, C.c_int, C.c_void_p,
                                        C.c_int, C.POINTER(C.c_uint64), C.c_double * 2]
+        L.oracle_flex_run.restype = C.c_int
+        L.oracle_flex_run.argtypes = [C.POINTER(_abi.ScanDesc), C.POINTER(_abi.FlexDesc), C.c_int,
+                                      C.c_int, C.c_void_p, C.c_int, C.POINTER(C.c_uint64),
+                                      C.c_int, C.c_void_p]
         L.oracle_sample.restype = C.c_int
         L.oracle_sample.argtypes = [C.POINTER(_abi.ScanDesc), C.c_int, C.c_void_p,
                                     C.c_int64, C.c_void_p]
@@ -89,6 +93,23 @@ def run_split(desc, col_begin: int = 0, col_end: int | None = None, threads: int
     _check(port().oracle_run_split(C.byref(d), col_begin, col_end, out.ctypes.data_as(C.c_void_p),
                                    threads, C.byref(steps), t))
     return out, int(steps.value), t[0], t[1]
+
+
+def flex_run(desc, flex, col_begin: int = 0, col_end: int | None = None, threads: int = 0,
+             state_column: int = -1):
+    """Relax a flexible scan with the FP64 port: (points, total_steps, states)."""
+    from mechafm_gb300 import _abi
+    d = desc.c
+    if col_end is None:
+        col_end = d.nx * d.ny
+    out = np.zeros((col_end - col_begin) * d.nz, dtype=_abi.POINT_DTYPE)
+    steps = C.c_uint64(0)
+    states = np.zeros((d.nz, d.n_atoms + 2, 3)) if state_column >= 0 else None
+    _check(port().oracle_flex_run(C.byref(d), C.byref(flex.c), col_begin, col_end,
+                                  out.ctypes.data_as(C.c_void_p), threads, C.byref(steps),
+                                  state_column,
+                                  states.ctypes.data_as(C.c_void_p) if states is not None else None))
+    return out, int(steps.value), states
 
 
 def sample(desc, pts: np.ndarray, what: int = 0) -> np.ndarray:

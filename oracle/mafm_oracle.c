@@ -908,3 +908,500 @@ int oracle_adjoint(const mafm_scan_desc* d, const mafm_point* pts, const double*
     ctx_free(&c);
     return 0;
 }
+
+/* ---- flexible molecules ---------------------------------------------------
+ * `flexible on`: every atom whose fixed flag is not 1 moves.  The interaction
+ * list is built in the reference's order (Simulation::buildInteractions,
+ * simulation.cpp:200-215: tip–surface, tip–dummy, bonds / angles / dihedrals /
+ * non-bonded pairs of buildSurfaceSurfaceInteractions :557-693, substrate and
+ * XY tethers of buildSubstrateInteractions :516-528) and evaluated into shared
+ * force / energy arrays exactly as the reference's integrators do
+ * (integrators.cpp:8-111), each term written as its eval() in
+ * interactions.cpp:15-51, 252-370. */
+
+enum { FI_LJ, FI_MORSE, FI_COUL, FI_TIPHARM, FI_XY, FI_SUB, FI_BOND, FI_ANGLE, FI_DIHED };
+
+typedef struct {
+    int type, ts;      /* ts: a tip–surface term (isTipSurface) */
+    int a[4];          /* System indices */
+    double p[6];
+    v3 shift;
+} FInt;
+
+typedef struct {
+    const mafm_scan_desc* d;
+    int na;
+    FInt* it;
+    int nit;
+    int* fixed;
+    v3* pos0;
+    double cell[3][3], cinv[3][3];
+} FCtx;
+
+static v3 vsub(v3 a, v3 b) { v3 r = {a.x - b.x, a.y - b.y, a.z - b.z}; return r; }
+static v3 vadd(v3 a, v3 b) { v3 r = {a.x + b.x, a.y + b.y, a.z + b.z}; return r; }
+static v3 vscal(double s, v3 a) { v3 r = {s * a.x, s * a.y, s * a.z}; return r; }
+static v3 vmul(v3 a, double s) { v3 r = {a.x * s, a.y * s, a.z * s}; return r; }
+static v3 vdiv(v3 a, double s) { v3 r = {a.x / s, a.y / s, a.z / s}; return r; }
+static double vdot(v3 a, v3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+static v3 vcross(v3 a, v3 b) {
+    v3 r = {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+    return r;
+}
+static v3 vnorm(v3 a) {
+    double l = len3(a);
+    v3 z = {0, 0, 0};
+    if (l > 1e-10) { v3 r = {a.x / l, a.y / l, a.z / l}; return r; }
+    return z;
+}
+
+static void fint_eval(const FCtx* c, const FInt* t, const v3* pos, v3* F, double* E) {
+    switch (t->type) {
+    case FI_LJ: {
+        int i1 = t->a[0], i2 = t->a[1];
+        v3 r = vsub(pos[i1], vadd(pos[i2], t->shift));
+        double r_sqr = r.x * r.x + r.y * r.y + r.z * r.z;
+        double r6 = r_sqr * r_sqr * r_sqr;
+        double ta = t->p[1] / (r6 * r6), tb = t->p[0] / r6;
+        double e = ta - tb;
+        v3 f = vscal((12 * ta - 6 * tb) / r_sqr, r);
+        E[i1] += e; E[i2] += e;
+        F[i1] = vadd(F[i1], f); F[i2] = vsub(F[i2], f);
+        break;
+    }
+    case FI_MORSE: {
+        int i1 = t->a[0], i2 = t->a[1];
+        v3 r = vsub(pos[i1], vadd(pos[i2], t->shift));
+        double rl = len3(r);
+        double d = exp(-t->p[1] * (rl - t->p[2]));
+        double e = t->p[0] * (d * d - 2 * d + 1);
+        double f_abs = 2 * t->p[0] * t->p[1] * (d * d - d);
+        v3 f = vscal(f_abs / rl, r);
+        E[i1] += e; E[i2] += e;
+        F[i1] = vadd(F[i1], f); F[i2] = vsub(F[i2], f);
+        break;
+    }
+    case FI_COUL: {
+        int i1 = t->a[0], i2 = t->a[1];
+        v3 r = vsub(pos[i1], pos[i2]);
+        double rl = len3(r);
+        double e = t->p[0] / rl;
+        v3 f = vscal(t->p[0] / (rl * rl * rl), r);
+        E[i1] += e; E[i2] += e;
+        F[i1] = vadd(F[i1], f); F[i2] = vsub(F[i2], f);
+        break;
+    }
+    case FI_TIPHARM: {
+        int i1 = t->a[0], i2 = t->a[1];
+        v3 rv = vsub(pos[i1], pos[i2]);
+        double r = sqrt(rv.x * rv.x + rv.y * rv.y);
+        double dr = r - t->p[1];
+        double e = t->p[0] * dr * dr;
+        v3 f = {0, 0, 0};
+        if (r > TOL) {
+            double s = -2 * t->p[0] * dr / r;
+            f.x = s * rv.x; f.y = s * rv.y; f.z = 0;
+        }
+        E[i1] += e; E[i2] += e;
+        F[i1] = vadd(F[i1], f); F[i2] = vsub(F[i2], f);
+        break;
+    }
+    case FI_XY: {
+        int i = t->a[0];
+        double rx = pos[i].x - t->p[1], ry = pos[i].y - t->p[2];
+        double r = sqrt(rx * rx + ry * ry);
+        double e = t->p[0] * r * r;
+        v3 f = {0, 0, 0};
+        if (r > TOL) { double s = -2 * t->p[0]; f.x = s * rx; f.y = s * ry; f.z = 0; }
+        E[i] += e;
+        F[i] = vadd(F[i], f);
+        break;
+    }
+    case FI_SUB: {
+        int i = t->a[0];
+        double mult = t->p[0], ulj = t->p[1], ushift = t->p[2], z0 = t->p[3], rc = t->p[4], sig = t->p[5];
+        double dz = pos[i].z - z0;
+        double sig_z = sig / dz;
+        double sig_z2 = sig_z * sig_z;
+        double sig_z4 = sig_z2 * sig_z2;
+        double sig_z10 = sig_z4 * sig_z4 * sig_z2;
+        double eterm = 0.0, fterm = 0.0;
+        if (dz <= rc) {
+            eterm += mult * (2. / 5 * sig_z10 - sig_z4) + ulj * dz * dz - ushift;
+            fterm += 4 * mult / dz * (sig_z10 - sig_z4) + 2 * ulj * dz;
+        }
+        F[i].z += fterm;
+        E[i] += eterm;
+        break;
+    }
+    case FI_BOND: {
+        int i1 = t->a[0], i2 = t->a[1];
+        v3 rv = vsub(pos[i1], pos[i2]);
+        double r = len3(rv);
+        double dr = r - t->p[1];
+        double e = t->p[0] * (dr * dr);
+        v3 f = vscal(-2 * t->p[0] * dr / r, rv);
+        E[i1] += e; E[i2] += e;
+        F[i1] = vadd(F[i1], f); F[i2] = vsub(F[i2], f);
+        break;
+    }
+    case FI_ANGLE: {
+        int sh = t->a[0], i1 = t->a[1], i2 = t->a[2];
+        v3 r1v = vsub(pos[i1], pos[sh]), r2v = vsub(pos[i2], pos[sh]);
+        double r1 = len3(r1v), r2 = len3(r2v);
+        double cos_t = vdot(r1v, r2v) / (r1 * r2);
+        if (cos_t > 1) cos_t = 1;
+        else if (cos_t < -1) cos_t = -1;
+        double theta = acos(cos_t);
+        double sin_t = sin(theta);
+        double d_theta = theta - t->p[1];
+        double fm = -2 * t->p[0] * d_theta / sin_t;
+        v3 f1 = vscal(-fm / r1, vsub(vdiv(r2v, r2), vdiv(vmul(r1v, cos_t), r1)));
+        v3 f2 = vscal(-fm / r2, vsub(vdiv(r1v, r1), vdiv(vmul(r2v, cos_t), r2)));
+        double e = t->p[0] * (d_theta * d_theta);
+        F[i1] = vadd(F[i1], f1);
+        F[i2] = vadd(F[i2], f2);
+        F[sh] = vsub(F[sh], vadd(f1, f2));
+        E[i1] += e; E[i2] += e; E[sh] += e;
+        break;
+    }
+    case FI_DIHED: {
+        int a1 = t->a[0], a2 = t->a[1], a3 = t->a[2], a4 = t->a[3];
+        v3 r12 = vsub(pos[a1], pos[a2]), r23v = vsub(pos[a2], pos[a3]), r43 = vsub(pos[a4], pos[a3]);
+        double r23 = len3(r23v);
+        v3 mv = vcross(r12, r23v), nv = vcross(r43, r23v);
+        double m = len3(mv), n = len3(nv);
+        double tan_s = vdot(nv, r12) * r23 / vdot(mv, nv);
+        double sigma = atan(tan_s);
+        double d_sigma = sigma - t->p[1];
+        double fm = 2 * t->p[0] * d_sigma;
+        v3 f1 = vscal(-fm * r23 / (m * m), mv);
+        v3 f2 = vscal(-fm, vsub(vscal(vdot(r43, r23v) / (n * n * r23), nv),
+                                vscal(((r23 * r23) + vdot(r12, r23v)) / (m * m * r23), mv)));
+        v3 f3 = vscal(-fm, vadd(vscal(vdot(r12, r23v) / (m * m * r23), mv),
+                                vscal(((r23 * r23) - vdot(r43, r23v)) / (n * n * r23), nv)));
+        v3 f4 = vscal(fm * r23 / (n * n), nv);
+        double e = t->p[0] * (d_sigma * d_sigma);
+        F[a1] = vadd(F[a1], f1); F[a2] = vadd(F[a2], f2);
+        F[a3] = vadd(F[a3], f3); F[a4] = vadd(F[a4], f4);
+        E[a1] += e; E[a2] += e; E[a3] += e; E[a4] += e;
+        break;
+    }
+    }
+    (void)c;
+}
+
+static void fl_eval(const FCtx* c, const v3* pos, v3* F, double* E, int ts_only) {
+    for (int i = 0; i < c->na; ++i) { F[i].x = F[i].y = F[i].z = 0; E[i] = 0; }
+    for (int q = 0; q < c->nit; ++q)
+        if (!ts_only || c->it[q].ts) fint_eval(c, &c->it[q], pos, F, E);
+}
+
+static int fl_push(FCtx* c, int* cap, FInt t) {
+    if (c->nit == *cap) {
+        *cap = *cap ? 2 * *cap : 256;
+        FInt* n = (FInt*)realloc(c->it, sizeof(FInt) * (size_t)*cap);
+        if (!n) return 1;
+        c->it = n;
+    }
+    c->it[c->nit++] = t;
+    return 0;
+}
+
+static int fctx_init(FCtx* c, const mafm_scan_desc* d, const mafm_flex_desc* f) {
+    memset(c, 0, sizeof *c);
+    c->d = d;
+    c->na = d->n_atoms + 2;
+    c->fixed = (int*)calloc((size_t)c->na, sizeof(int));
+    c->pos0 = (v3*)calloc((size_t)c->na, sizeof(v3));
+    if (!c->fixed || !c->pos0) return MAFM_E_NOMEM;
+    c->fixed[0] = 1;
+    for (int a = 0; a < d->n_atoms; ++a) {
+        c->fixed[a + 2] = f->fixed[a];
+        c->pos0[a + 2].x = d->pos[3 * a]; c->pos0[a + 2].y = d->pos[3 * a + 1]; c->pos0[a + 2].z = d->pos[3 * a + 2];
+    }
+    for (int r = 0; r < 3; ++r)
+        for (int k = 0; k < 3; ++k) c->cell[r][k] = d->cell[3 * r + k];
+    if (d->tip_pbc) inv3(c->cell, c->cinv);
+    int cap = 0;
+    FInt t;
+    /* buildTipSurfaceInteractions (simulation.cpp:297-320) */
+    for (int ia = -1; ia <= 1; ++ia)
+        for (int ib = -1; ib <= 1; ++ib) {
+            if (!d->vdw_pbc && (ia != 0 || ib != 0)) continue;
+            v3 sh = {0, 0, 0};
+            if (d->vdw_pbc) {
+                sh.x = ia * c->cell[0][0] + ib * c->cell[0][1];
+                sh.y = ia * c->cell[1][0] + ib * c->cell[1][1];
+                sh.z = ia * c->cell[2][0] + ib * c->cell[2][1];
+            }
+            for (int a = 0; a < d->n_atoms; ++a) {
+                const mafm_pair* pr = &d->tip_pair[d->type[a]];
+                memset(&t, 0, sizeof t);
+                t.type = pr->kind == MAFM_PAIR_LJ ? FI_LJ : FI_MORSE;
+                t.ts = 1; t.a[0] = 1; t.a[1] = a + 2; t.shift = sh;
+                for (int k = 0; k < 3; ++k) t.p[k] = pr->p[k];
+                if (fl_push(c, &cap, t)) return MAFM_E_NOMEM;
+                if (!d->vdw_pbc && d->coulomb && d->tip_charge != 0 && d->charge[a] != 0) {
+                    memset(&t, 0, sizeof t);
+                    t.type = FI_COUL; t.ts = 1; t.a[0] = 1; t.a[1] = a + 2;
+                    t.p[0] = d->qbase * d->tip_charge * d->charge[a];
+                    if (fl_push(c, &cap, t)) return MAFM_E_NOMEM;
+                }
+            }
+        }
+    /* buildTipDummyInteractions (simulation.cpp:503-515) */
+    memset(&t, 0, sizeof t);
+    t.type = d->dummy_pair.kind == MAFM_PAIR_LJ ? FI_LJ : FI_MORSE;
+    t.a[0] = 0; t.a[1] = 1;
+    for (int k = 0; k < 3; ++k) t.p[k] = d->dummy_pair.p[k];
+    if (fl_push(c, &cap, t)) return MAFM_E_NOMEM;
+    if (d->tip_dummy_coulomb && d->dummy_charge != 0 && d->tip_charge != 0) {
+        memset(&t, 0, sizeof t);
+        t.type = FI_COUL; t.a[0] = 0; t.a[1] = 1;
+        t.p[0] = d->qbase * d->dummy_charge * d->tip_charge;
+        if (fl_push(c, &cap, t)) return MAFM_E_NOMEM;
+    }
+    memset(&t, 0, sizeof t);
+    t.type = FI_TIPHARM; t.a[0] = 0; t.a[1] = 1; t.p[0] = d->harm_k; t.p[1] = d->harm_r0;
+    if (fl_push(c, &cap, t)) return MAFM_E_NOMEM;
+    /* buildSurfaceSurfaceInteractions: bonds, angles, dihedrals, pairs */
+    for (int b = 0; b < f->n_bonds; ++b) {
+        memset(&t, 0, sizeof t);
+        t.type = FI_BOND; t.a[0] = f->bond_atoms[2 * b] + 2; t.a[1] = f->bond_atoms[2 * b + 1] + 2;
+        t.p[0] = f->bond_param[2 * b]; t.p[1] = f->bond_param[2 * b + 1];
+        if (fl_push(c, &cap, t)) return MAFM_E_NOMEM;
+    }
+    for (int g = 0; g < f->n_angles; ++g) {
+        memset(&t, 0, sizeof t);
+        t.type = FI_ANGLE;
+        for (int k = 0; k < 3; ++k) t.a[k] = f->angle_atoms[3 * g + k] + 2;
+        t.p[0] = f->angle_param[2 * g]; t.p[1] = f->angle_param[2 * g + 1];
+        if (fl_push(c, &cap, t)) return MAFM_E_NOMEM;
+    }
+    for (int g = 0; g < f->n_dihedrals; ++g) {
+        memset(&t, 0, sizeof t);
+        t.type = FI_DIHED;
+        for (int k = 0; k < 4; ++k) t.a[k] = f->dihedral_atoms[4 * g + k] + 2;
+        t.p[0] = f->dihedral_param[2 * g]; t.p[1] = f->dihedral_param[2 * g + 1];
+        if (fl_push(c, &cap, t)) return MAFM_E_NOMEM;
+    }
+    for (int q = 0; q < f->n_pairs; ++q) {
+        memset(&t, 0, sizeof t);
+        t.type = f->pair_vdw[q].kind == MAFM_PAIR_LJ ? FI_LJ : FI_MORSE;
+        t.a[0] = f->pair_atoms[2 * q] + 2; t.a[1] = f->pair_atoms[2 * q + 1] + 2;
+        for (int k = 0; k < 3; ++k) t.p[k] = f->pair_vdw[q].p[k];
+        if (fl_push(c, &cap, t)) return MAFM_E_NOMEM;
+        if (f->pair_qq && f->pair_qq[q] != 0) {
+            memset(&t, 0, sizeof t);
+            t.type = FI_COUL; t.a[0] = f->pair_atoms[2 * q] + 2; t.a[1] = f->pair_atoms[2 * q + 1] + 2;
+            t.p[0] = f->pair_qq[q];
+            if (fl_push(c, &cap, t)) return MAFM_E_NOMEM;
+        }
+    }
+    /* buildSubstrateInteractions; SubstrateInteraction ctor interactions.hpp:222-229 */
+    double eps = f->substrate[0], sig = f->substrate[1], lam = f->substrate[2], rc = f->substrate[3];
+    double mult = 2 * PI * eps * pow(sig / lam, 2);
+    double ulj = (PI / (lam * lam)) * 4 * eps * (pow(sig / rc, 12) - pow(sig / rc, 6));
+    double ushift = mult * ((12. / 5) * pow(sig / rc, 10) - 3 * pow(sig / rc, 4));
+    for (int i = 2; i < c->na; ++i) {
+        memset(&t, 0, sizeof t);
+        t.type = FI_SUB; t.a[0] = i;
+        t.p[0] = mult; t.p[1] = ulj; t.p[2] = ushift; t.p[3] = -sig; t.p[4] = rc; t.p[5] = sig;
+        if (fl_push(c, &cap, t)) return MAFM_E_NOMEM;
+        if (c->fixed[i] == 2) {
+            memset(&t, 0, sizeof t);
+            t.type = FI_XY; t.a[0] = i; t.p[0] = f->substrate[4];
+            t.p[1] = c->pos0[i].x; t.p[2] = c->pos0[i].y;
+            if (fl_push(c, &cap, t)) return MAFM_E_NOMEM;
+        }
+    }
+    return 0;
+}
+
+static void fctx_free(FCtx* c) {
+    free(c->it); free(c->fixed); free(c->pos0);
+}
+
+typedef struct {
+    v3 *pos, *vel, *F, *p2, *v2, *p3, *v3b, *p4, *v4, *f1, *f2, *f3, *f4;
+    double *E, *e1, *e2, *e3, *e4;
+} FState;
+
+/* one integrator step (integrators.cpp:8-111): forces_/energies_ in F/E */
+static void fl_step(const FCtx* c, FState* s, double dt) {
+    const int n = c->na;
+    const mafm_scan_desc* d = c->d;
+    if (d->integrator == MAFM_INT_EULER) {
+        fl_eval(c, s->pos, s->F, s->E, 0);
+        for (int i = 0; i < n; ++i)
+            if (c->fixed[i] != 1) {
+                s->pos[i] = vadd(s->pos[i], vscal(dt, s->vel[i]));
+                s->vel[i] = vadd(s->vel[i], vdiv(vscal(dt, s->F[i]), 1.0));
+            }
+    } else if (d->integrator == MAFM_INT_MIDPOINT) {
+        memcpy(s->p2, s->pos, sizeof(v3) * n);
+        memcpy(s->v2, s->vel, sizeof(v3) * n);
+        fl_eval(c, s->pos, s->f1, s->e1, 0);
+        for (int i = 0; i < n; ++i)
+            if (c->fixed[i] != 1) {
+                s->p2[i] = vadd(s->p2[i], vscal(dt / 2, s->vel[i]));
+                s->v2[i] = vadd(s->v2[i], vdiv(vscal(dt / 2, s->f1[i]), 1.0));
+            }
+        fl_eval(c, s->p2, s->f2, s->e2, 0);
+        for (int i = 0; i < n; ++i) {
+            if (c->fixed[i] != 1) {
+                s->pos[i] = vadd(s->pos[i], vscal(dt, s->v2[i]));
+                s->vel[i] = vadd(s->vel[i], vdiv(vscal(dt, s->f2[i]), 1.0));
+            }
+            s->F[i] = s->f2[i];
+            s->E[i] = s->e2[i];
+        }
+    } else {
+        memcpy(s->p2, s->pos, sizeof(v3) * n); memcpy(s->p3, s->pos, sizeof(v3) * n);
+        memcpy(s->p4, s->pos, sizeof(v3) * n);
+        memcpy(s->v2, s->vel, sizeof(v3) * n); memcpy(s->v3b, s->vel, sizeof(v3) * n);
+        memcpy(s->v4, s->vel, sizeof(v3) * n);
+        fl_eval(c, s->pos, s->f1, s->e1, 0);
+        for (int i = 0; i < n; ++i)
+            if (c->fixed[i] != 1) {
+                s->p2[i] = vadd(s->p2[i], vscal(dt / 2, s->vel[i]));
+                s->v2[i] = vadd(s->v2[i], vdiv(vscal(dt / 2, s->f1[i]), 1.0));
+            }
+        fl_eval(c, s->p2, s->f2, s->e2, 0);
+        for (int i = 0; i < n; ++i)
+            if (c->fixed[i] != 1) {
+                s->p3[i] = vadd(s->p3[i], vscal(dt / 2, s->v2[i]));
+                s->v3b[i] = vadd(s->v3b[i], vdiv(vscal(dt / 2, s->f2[i]), 1.0));
+            }
+        fl_eval(c, s->p3, s->f3, s->e3, 0);
+        for (int i = 0; i < n; ++i)
+            if (c->fixed[i] != 1) {
+                s->p4[i] = vadd(s->p4[i], vscal(dt, s->v3b[i]));
+                s->v4[i] = vadd(s->v4[i], vdiv(vscal(dt, s->f3[i]), 1.0));
+            }
+        fl_eval(c, s->p4, s->f4, s->e4, 0);
+        for (int i = 0; i < n; ++i) {
+            v3 fs = vadd(vadd(vadd(s->f1[i], vscal(2, s->f2[i])), vscal(2, s->f3[i])), s->f4[i]);
+            if (c->fixed[i] != 1) {
+                v3 vs = vadd(vadd(vadd(s->vel[i], vscal(2, s->v2[i])), vscal(2, s->v3b[i])), s->v4[i]);
+                s->pos[i] = vadd(s->pos[i], vscal(dt / 6, vs));
+                s->vel[i] = vadd(s->vel[i], vdiv(vscal(dt / 6, fs), 1.0));
+            }
+            s->F[i] = vdiv(fs, 6);
+            s->E[i] = (s->e1[i] + 2 * s->e2[i] + 2 * s->e3[i] + s->e4[i]) / 6;
+        }
+    }
+}
+
+static int fl_converged(const mafm_scan_desc* d, v3 F, double ediff) {
+    return converged(d, F, ediff);
+}
+
+/* FIREMinimisation / SDMinimisation over all atoms (minimiser.cpp:39-129) */
+static int fl_minimise(const FCtx* c, FState* s) {
+    const mafm_scan_desc* d = c->d;
+    const int n = c->na;
+    if (d->minimiser == MAFM_MIN_SD) {
+        double prev = -10e6;
+        int k = 1;
+        for (; k < d->maxsteps; ++k) {
+            prev = s->E[1];
+            fl_eval(c, s->pos, s->F, s->E, 0);
+            if (fl_converged(d, s->F[1], s->E[1] - prev)) break;
+            for (int i = 0; i < n; ++i)
+                if (c->fixed[i] != 1) s->pos[i] = vadd(s->pos[i], vscal(d->dt, s->F[i]));
+        }
+        (void)prev;
+        return k;
+    }
+    double alpha = 0.1, dt = d->dt, dt_max = 10 * d->dt, prev = -10e6;
+    int n_non_neg = 0, k = 1;
+    for (; k < d->maxsteps; ++k) {
+        prev = s->E[1];
+        fl_step(c, s, dt);
+        if (fl_converged(d, s->F[1], s->E[1] - prev)) break;
+        double p = 0;
+        for (int i = 0; i < n; ++i) {
+            p += vdot(s->vel[i], s->F[i]);
+            if (c->fixed[i] != 1)
+                s->vel[i] = vadd(vscal(1 - alpha, s->vel[i]), vmul(vscal(alpha, vnorm(s->F[i])), len3(s->vel[i])));
+        }
+        if (p < 0) {
+            for (int i = 0; i < n; ++i) s->vel[i].x = s->vel[i].y = s->vel[i].z = 0;
+            n_non_neg = 0;
+            dt *= 0.5;
+            alpha = 0.1;
+        } else {
+            if (n_non_neg > 5) {
+                dt = fmin(dt * 1.1, dt_max);
+                alpha *= 0.99;
+            }
+            n_non_neg++;
+        }
+    }
+    (void)prev;
+    return k;
+}
+
+/* Relax columns [col_begin, col_end) of a flexible scan; states (optional)
+ * receives every atom's position after each height of column state_column. */
+int oracle_flex_run(const mafm_scan_desc* d, const mafm_flex_desc* f, int col_begin, int col_end,
+                    mafm_point* out, int nthreads, uint64_t* total_steps, int state_column,
+                    double* states) {
+    FCtx c;
+    int st = fctx_init(&c, d, f);
+    if (st) { fctx_free(&c); return st; }
+    unsigned long long steps = 0;
+    const int n = c.na;
+#pragma omp parallel for schedule(dynamic, 1) reduction(+ : steps) num_threads(nthreads > 0 ? nthreads : omp_get_max_threads())
+    for (int col = col_begin; col < col_end; ++col) {
+        FState s;
+        v3** vs[] = {&s.pos, &s.vel, &s.F, &s.p2, &s.v2, &s.p3, &s.v3b, &s.p4, &s.v4, &s.f1, &s.f2, &s.f3, &s.f4};
+        for (size_t q = 0; q < sizeof vs / sizeof vs[0]; ++q) *vs[q] = (v3*)calloc((size_t)n, sizeof(v3));
+        double** es[] = {&s.E, &s.e1, &s.e2, &s.e3, &s.e4};
+        for (size_t q = 0; q < sizeof es / sizeof es[0]; ++q) *es[q] = (double*)calloc((size_t)n, sizeof(double));
+        memcpy(s.pos, c.pos0, sizeof(v3) * n);
+        const int i = col / d->ny, j = col % d->ny;
+        double x = i * d->dx, y = j * d->dy, ox = x, oy = y;
+        if (d->tip_pbc) {
+            v3 t = {x - d->offset[0], y - d->offset[1], 0 - d->offset[2]};
+            v3 cn = mulv(c.cinv, t);
+            cn.x -= floor(cn.x);
+            cn.y -= floor(cn.y);
+            v3 pb = mulv(c.cell, cn);
+            ox = pb.x + d->offset[0];
+            oy = pb.y + d->offset[1];
+        }
+        s.pos[0].x = ox; s.pos[0].y = oy; s.pos[1].x = ox; s.pos[1].y = oy;
+        s.pos[0].z = d->zhigh;
+        s.pos[1].z = d->zhigh - d->tip_dummy_d;
+        for (int k = 0; k < d->nz; ++k) {
+            int nst = fl_minimise(&c, &s);
+            v3* Fo = (v3*)calloc((size_t)n, sizeof(v3));
+            double* Eo = (double*)calloc((size_t)n, sizeof(double));
+            fl_eval(&c, s.pos, Fo, Eo, 1);
+            mafm_point* r = out + (size_t)(col - col_begin) * d->nz + k;
+            r->tip[0] = s.pos[1].x; r->tip[1] = s.pos[1].y; r->tip[2] = s.pos[1].z;
+            r->force[0] = Fo[1].x; r->force[1] = Fo[1].y; r->force[2] = Fo[1].z;
+            r->energy = Eo[1];
+            r->steps = nst;
+            r->status = nst >= d->maxsteps ? MAFM_PT_MAXSTEPS : 0;
+            free(Fo); free(Eo);
+            steps += (unsigned long long)nst;
+            if (states && col == state_column)
+                for (int a = 0; a < n; ++a) {
+                    states[((size_t)k * n + a) * 3] = s.pos[a].x;
+                    states[((size_t)k * n + a) * 3 + 1] = s.pos[a].y;
+                    states[((size_t)k * n + a) * 3 + 2] = s.pos[a].z;
+                }
+            s.pos[0].z -= d->dz;
+            s.pos[1].z -= d->dz;
+        }
+        for (size_t q = 0; q < sizeof vs / sizeof vs[0]; ++q) free(*vs[q]);
+        for (size_t q = 0; q < sizeof es / sizeof es[0]; ++q) free(*es[q]);
+    }
+    if (total_steps) *total_steps = steps;
+    fctx_free(&c);
+    return 0;
+}

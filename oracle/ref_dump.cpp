@@ -13,6 +13,7 @@
 //
 // Modes
 //   ref_dump scan   INPUT OUT.bin [i0 i1 j0 j1]   per-point records (25 doubles)
+//   ref_dump states INPUT OUT.bin i j              every atom after each height of column (i, j)
 //   ref_dump system INPUT OUT.txt                 prepared System after initialize()
 //   ref_dump sample_ts INPUT POINTS.bin OUT.bin   tip-surface F,E at given tip positions
 //   ref_dump sample_es INPUT POINTS.bin OUT.bin   external-field F,E at given tip positions
@@ -118,6 +119,31 @@ int main(int argc, char** argv) {
         for (int i = i0; i < i1; ++i)
             for (int j = j0; j < j1; ++j)
                 column(sim, i, j, out.data() + ((size_t)(i - i0) * nj + (j - j0)) * np.z * 25);
+        FILE* f = fopen(argv[3], "wb");
+        fwrite(out.data(), sizeof(double), out.size(), f);
+        fclose(f);
+        return 0;
+    }
+    if (mode == "states") {
+        // every atom's position after each height of column (i, j)
+        if (argc < 6) return 2;
+        const int i = atoi(argv[4]), j = atoi(argv[5]);
+        const InputOptions& o = sim.options_;
+        System s = sim.system;
+        if (o.rigidgrid) s.setTipPbc(false);
+        s.setDummyXY(i * o.dx, j * o.dy);
+        s.setDummyZ(o.zhigh);
+        std::vector<double> out;
+        for (int k = 0; k < np.z; ++k) {
+            if (o.minimiser_type == STEEPEST_DESCENT) SDMinimisation(s, o);
+            else FIREMinimisation(s, o);
+            for (int a = 0; a < s.n_atoms_; ++a) {
+                out.push_back(s.positions_[a].x);
+                out.push_back(s.positions_[a].y);
+                out.push_back(s.positions_[a].z);
+            }
+            s.lowerTip(o.dz);
+        }
         FILE* f = fopen(argv[3], "wb");
         fwrite(out.data(), sizeof(double), out.size(), f);
         fclose(f);

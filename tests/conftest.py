@@ -22,7 +22,10 @@ def _manifest():
 
 
 MANIFEST = _manifest()
-POINT_CASES = sorted(k for k, v in MANIFEST.items() if "error" not in v and not v.get("cli"))
+POINT_CASES = sorted(k for k, v in MANIFEST.items()
+                     if "error" not in v and not v.get("cli") and v.get("sample") != "states")
+# flexible molecules: relaxed through mafm_flex_* with the atoms' states
+FLEX_CASES = sorted(k for k, v in MANIFEST.items() if v.get("sample") == "states")
 ERROR_CASES = sorted(k for k, v in MANIFEST.items() if "error" in v)
 
 

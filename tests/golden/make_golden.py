@@ -86,6 +86,11 @@ def cases():
     c.append(("graphene_ovwrt", ow, (50, 53, 20, 23), None))
     c.append(("cluster_maxsteps", synth.cluster_60(zlow=9.0, maxsteps="40"),
               (180, 183, 180, 183), None))
+    # flexible molecule (bonds, angles, dihedrals, non-bonded pairs between
+    # fragments, substrate, XY tethers); the middle column's atom states too
+    c.append(("flex_naph", synth.flexible_naphthalene(), (0, 3, 0, 3), "states"))
+    c.append(("flex_naph_rk4", synth.flexible_naphthalene(integrator="rk4", zlow=9.0),
+              (0, 3, 0, 3), "states"))
     return c
 
 
@@ -107,6 +112,7 @@ def cli_cases():
         ("cli_pbc", synth.graphene_72(area=20.0, step=10.0, zhigh=10.0, zlow=9.8, dz=0.1,
                                       vdw_pbc="on", cell_a=_vec(ca), cell_b=_vec(cb),
                                       cell_c=_vec(cc))),
+        ("cli_flex", synth.flexible_naphthalene(area=1.0, step=0.5, zhigh=10.0, zlow=9.6, dz=0.2)),
     ]
 
 
@@ -126,6 +132,14 @@ def make_cli_fixture(name, spec):
                 rows += [fn + "\t" + l.rstrip("\n") for l in f]
     with open(os.path.join(folder, "cli_rows.txt"), "w") as f:
         f.write("\n".join(sorted(rows)) + "\n")
+    states = []
+    for fn in sorted(os.listdir(out)):
+        if fn.startswith("state_"):
+            with open(os.path.join(out, fn)) as f:
+                states += [fn + "\t" + l.rstrip("\n") for l in f]
+    if states:
+        with open(os.path.join(folder, "cli_states.txt"), "w") as f:
+            f.write("\n".join(states) + "\n")
     with open(os.path.join(out, "statistics.txt")) as f:
         stats = f.readlines()[:4]
     with open(os.path.join(folder, "cli_statistics_head.txt"), "w") as f:
@@ -179,7 +193,17 @@ def main(only=()):
         out["sys_offset"] = np.array(sysinfo["offset"])
         out["sys_n_points"] = np.array(sysinfo["n_points"], dtype=np.int32)
         out["sys_xyz_charges"] = np.array(int(sysinfo["xyz_charges"]), dtype=np.int32)
-        if sample:
+        if sample == "states":
+            n = out["sys_n_points"]
+            i, j = (n[0] * n[1] // 2) // n[1], (n[0] * n[1] // 2) % n[1]
+            sbin = os.path.join(folder, "_states.bin")
+            subprocess.run([oracle.REF_DUMP, "states", os.path.abspath(inp), sbin, str(i), str(j)],
+                           check=True, cwd=folder, stdout=subprocess.DEVNULL,
+                           stderr=subprocess.DEVNULL)
+            out["states"] = np.fromfile(sbin).reshape(int(n[2]), -1, 3)
+            out["states_column"] = np.array([i, j], dtype=np.int32)
+            os.remove(sbin)
+        elif sample:
             pts = sample_points(name, spec)
             fe = oracle.ref_sample(inp, pts, sample, os.path.join(folder, "_s"))
             for ext in (".pts", ".fe"):

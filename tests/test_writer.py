@@ -35,7 +35,10 @@ def test_scan_files_match_reference_executable(name, use_gzip, tmp_path):
     folder = os.path.join(GOLDEN, name)
     inp = Input(os.path.join(folder, MANIFEST[name]["input"]))
     desc = inp.desc()
-    pts, steps = oracle.run(desc)
+    if desc.c.flexible:
+        pts, steps, _ = oracle.flex_run(desc, inp.flex_desc())
+    else:
+        pts, steps = oracle.run(desc)
     inp.write_output(pts, str(tmp_path), gzip=use_gzip)
     want = open(os.path.join(folder, "cli_rows.txt")).read().splitlines()
     assert rows_of(str(tmp_path)) == want
@@ -43,3 +46,22 @@ def test_scan_files_match_reference_executable(name, use_gzip, tmp_path):
     _abi.check(_abi.lib().mafm_write_statistics(inp.handle, out.encode(), steps, 1.0, 1.0))
     head = open(os.path.join(tmp_path, "statistics.txt")).readlines()[:4]
     assert head == open(os.path.join(folder, "cli_statistics_head.txt")).readlines()
+
+
+def test_state_files_match_reference_executable(tmp_path):
+    """System::makeXYZFile's state_*.xyz files of the middle pixel of a
+    flexible scan (simulation.cpp:114-116), written by mafm_write_states from
+    the oracle's atom states, equal the reference executable's."""
+    folder = os.path.join(GOLDEN, "cli_flex")
+    inp = Input(os.path.join(folder, MANIFEST["cli_flex"]["input"]))
+    desc = inp.desc()
+    col = desc.c.nx * desc.c.ny // 2
+    _, _, states = oracle.flex_run(desc, inp.flex_desc(), col, col + 1, state_column=col)
+    out = str(tmp_path) + "/"
+    _abi.check(_abi.lib().mafm_write_states(inp.handle, states.ctypes.data, col, out.encode()))
+    got = []
+    for fn in sorted(os.listdir(tmp_path)):
+        if fn.startswith("state_"):
+            got += [fn + "\t" + l.rstrip("\n") for l in open(os.path.join(tmp_path, fn))]
+    want = open(os.path.join(folder, "cli_states.txt")).read().splitlines()
+    assert got == want
