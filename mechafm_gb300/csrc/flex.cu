@@ -895,6 +895,7 @@ extern "C" int mafm_flex_run(mafm_flex* s, int32_t col_begin, int32_t col_end, m
                 cuda_check(cudaMalloc(&tmp_states, states_bytes), "cudaMalloc");
                 frees.b = tmp_states;
                 dstates = static_cast<double*>(tmp_states);
+                cuda_check(cudaMemsetAsync(tmp_states, 0, states_bytes, st), "memset states");
             }
         }
         FlexKernelArgs A{};
