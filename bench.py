@@ -87,6 +87,8 @@ def parse():
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-tune", action="store_true", help="default launch shape, no autotuner")
     ap.add_argument("--lanes", type=int, default=0, help="force lanes per column")
+    ap.add_argument("--tile", type=int, default=0, help="force columns per tile")
+    ap.add_argument("--block", type=int, default=0, help="force threads per block")
     ap.add_argument("--pixels", type=int, default=0, help="pixels per side (profiling)")
     ap.add_argument("--sweep", action="store_true",
                     help="also time every lanes-per-column value (stderr)")
@@ -509,9 +511,9 @@ def ours(args, rank, world, local):
         t_grid = time.perf_counter() - t0
 
     # launch shape: the autotuner (on at most 32 scans of a batch)
-    opts = _abi.RunOpts(_abi.FP32C, args.lanes, 0, 0, 0, 0)
+    opts = _abi.RunOpts(_abi.FP32C, args.lanes, args.block, args.tile, 0, 0)
     tune_ms = None
-    if not args.no_tune and not args.lanes:
+    if not args.no_tune and not (args.lanes or args.block or args.tile):
         best = _abi.RunOpts()
         tms = C.c_double()
         _abi.check(L.mafm_autotune(handles, min(n, 32), C.byref(best), C.byref(tms), sptr))
@@ -606,15 +608,17 @@ def ours(args, rank, world, local):
     ms_adj = time_events(stream, adj, 2) if adjoint else 0.0
 
     if args.sweep and rank == 0:
-        for lanes in (1, 2, 4, 8, 16, 32):
-            o = _abi.RunOpts(_abi.FP32C, lanes, 0, 0, 0, 0)
-            p2 = C.c_void_p()
-            _abi.check(L.mafm_plan_create(handles, n, C.byref(o), optrs, C.byref(p2)))
-            _abi.check(L.mafm_plan_launch(p2, sptr))
-            t = time_events(stream, lambda: _abi.check(L.mafm_plan_launch(p2, sptr)))
-            L.mafm_plan_destroy(p2)
-            print(json.dumps({"sweep_lanes": lanes, "ms": t, "points_per_s": n_pts / t * 1e3}),
-                  file=sys.stderr)
+        for lanes in (1, 2, 4):
+            for block in (128, 256):
+                for tile in sorted({1, 2, 4, 8, 32 // lanes, 128 // lanes}):
+                    o = _abi.RunOpts(_abi.FP32C, lanes, block, tile, 0, 0)
+                    p2 = C.c_void_p()
+                    _abi.check(L.mafm_plan_create(handles, n, C.byref(o), optrs, C.byref(p2)))
+                    _abi.check(L.mafm_plan_launch(p2, sptr))
+                    t = time_events(stream, lambda: _abi.check(L.mafm_plan_launch(p2, sptr)), 2)
+                    L.mafm_plan_destroy(p2)
+                    print(json.dumps({"sweep_lanes": lanes, "block": block, "tile": tile, "ms": t,
+                                      "points_per_s": n_pts / t * 1e3}), file=sys.stderr)
 
     # e2e through the public API from host memory
     h2d = 0

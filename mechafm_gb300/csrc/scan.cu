@@ -627,7 +627,12 @@ void check_device_errors(const RunCounters& c) {
 }
 
 // Default FP32 launch shape: enough lanes per column that every SM gets work
-// several times over, one column per group per tile.
+// several times over; one column per tile, so that a group takes its next
+// column from the shared queue when it frees up and the queue (in descending
+// expected cost) stays shared until the last columns: longer tiles reserve
+// columns for a warp's lanes early and leave the end of a launch statically
+// assigned (measured on the 401 x 401 cluster at G = 1: 100 ms at one column
+// per tile, 114 ms at 32).
 Relax32Config default_config(long long n_cols, int max_terms, const mafm_run_opts* o) {
     Relax32Config c{};
     c.block = (o && o->block_threads) ? o->block_threads : 256;
@@ -636,7 +641,7 @@ Relax32Config default_config(long long n_cols, int max_terms, const mafm_run_opt
     while (G < 32 && n_cols * G < 4 * lanes_cap) G *= 2;
     if (max_terms <= 1) G = 1;
     c.lanes = (o && o->lanes_per_column) ? o->lanes_per_column : G;
-    c.cols_per_tile = (o && o->columns_per_tile) ? o->columns_per_tile : 32 / c.lanes;
+    c.cols_per_tile = (o && o->columns_per_tile) ? o->columns_per_tile : 1;
     // Shared slice per warp, in 32 B term slots: the paired records of up to
     // 400 terms (each kind's run padded to even: + 2); 12.9 KB per warp keeps
     // two 8-warp blocks per SM.
@@ -1129,8 +1134,8 @@ int mafm_plan_config(const mafm_plan* plan, mafm_run_opts* opts) {
 }
 
 // Time launch shapes on the scans themselves and keep the fastest: lanes per
-// column first (block 256, one column per group per tile), then block size and
-// tile length around the best lane count.
+// column first (block 256, one column per tile), then block size and tile
+// length around the best lane count.
 int mafm_autotune(mafm_scan* const* scans, int32_t n_scans, mafm_run_opts* best, double* best_ms,
                   void* stream) {
     return guarded([&] {
@@ -1179,16 +1184,16 @@ int mafm_autotune(mafm_scan* const* scans, int32_t n_scans, mafm_run_opts* best,
         for (int G : lane_set) {
             if (G > 1 && G > std::max(max_terms, 1)) break;
             o.lanes_per_column = G;
-            o.columns_per_tile = 32 / G;
+            o.columns_per_tile = 1;
             const double ms = time_opts(o);
             if (ms < keep_ms) { keep_ms = ms; keep = o; }
         }
         mafm_run_opts base = keep;
         for (int block : {128, 256}) {
-            for (int mult : {1, 4}) {
+            for (int tile : {1, 4}) {
                 mafm_run_opts c = base;
                 c.block_threads = block;
-                c.columns_per_tile = (32 / base.lanes_per_column) * mult;
+                c.columns_per_tile = tile;
                 if (block == base.block_threads && c.columns_per_tile == base.columns_per_tile) continue;
                 const double ms = time_opts(c);
                 if (ms < keep_ms) { keep_ms = ms; keep = c; }
