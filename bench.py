@@ -608,7 +608,7 @@ def ours(args, rank, world, local):
     ms_adj = time_events(stream, adj, 2) if adjoint else 0.0
 
     if args.sweep and rank == 0:
-        for lanes in (1, 2, 4):
+        for lanes in (1, 2, 4, 8):
             for block in (128, 256):
                 for tile in sorted({1, 2, 4, 8, 32 // lanes, 128 // lanes}):
                     o = _abi.RunOpts(_abi.FP32C, lanes, block, tile, 0, 0)

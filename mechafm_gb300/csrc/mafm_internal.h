@@ -197,6 +197,6 @@ long long scan_columns(const mafm_scan* s);
 int scan_direct_terms(const mafm_scan* s);
 bool scan_fp32_ready(const mafm_scan* s);   // FP32 tables on the device (rigid grid built if used)
 BatchScan scan_batch_entry(const mafm_scan* s, mafm_point* out);
-Relax32Config relax32_config(long long n_cols, int max_terms, const mafm_run_opts* o);
+Relax32Config relax32_config(long long n_cols, int max_terms, const mafm_run_opts* o, int n_scans);
 void check_run_errors(const RunCounters& c);
 }  // namespace mafm

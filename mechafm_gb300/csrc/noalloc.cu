@@ -105,7 +105,7 @@ extern "C" int mafm_run_batch_noalloc(mafm_scan* const* scans, int32_t n_scans,
             total_cols += scan_columns(scans[i]);
             max_terms = max_terms > scan_direct_terms(scans[i]) ? max_terms : scan_direct_terms(scans[i]);
         }
-        const Relax32Config cfg = relax32_config(total_cols, max_terms, opts);
+        const Relax32Config cfg = relax32_config(total_cols, max_terms, opts, n_scans);
         cudaStream_t st = (cudaStream_t)stream;
         unsigned char* base = static_cast<unsigned char*>(scratch_address(device));
         RunCounters* ctr = reinterpret_cast<RunCounters*>(base);

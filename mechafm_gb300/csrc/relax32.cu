@@ -223,9 +223,10 @@ __device__ __forceinline__ void unit32(const TermPair32& t, const Tip2& p, bool 
 // Units [begin, end) of one kind: lane lg of the group takes begin + lg,
 // begin + lg + G, ...; kChunk / 2 units (kChunk terms) are summed plainly
 // before one compensated add.  Full chunks run without bounds tests.
-template <int G, bool kMorse>
+template <int G, bool kMorse, bool kCoul>
 __device__ __forceinline__ void sum_units(const TermPair32* units, int begin, int end, int lg,
-                                          const Tip2& tp, bool coul, Acc& acc) {
+                                          const Tip2& tp, Acc& acc) {
+    constexpr bool coul = kCoul;
     constexpr int kUnits = kChunk / 2;
     int u0 = begin + lg;
     for (; u0 + (kUnits - 1) * G < end; u0 += G * kUnits) {
@@ -252,35 +253,53 @@ __device__ __forceinline__ void sum_units(const TermPair32* units, int begin, in
 // Units [begin, end) of one kind for NB tip positions that share x and y (a
 // strip of NB nodes of one grid column): the x and y separations and
 // dx^2 + dy^2 are computed once per record for all NB positions.
-template <bool kMorse, int NB>
+// One record for the NB positions of a strip.
+template <bool kMorse, bool kCoul, int NB>
+__device__ __forceinline__ void unit32_strip(const TermPair32& t, float2 hx, float2 hy,
+                                             const float2 (&hz)[NB], Sum2 (&sm)[NB]) {
+    const float4 xy = t.xy, zq = t.zq;
+    const float2 dx = add2(hx, make_float2(xy.x, xy.y));
+    const float2 dy = add2(hy, make_float2(xy.z, xy.w));
+    const float2 dxy2 = fma2(dy, dy, mul2(dx, dx));
+    const float2 naz = make_float2(zq.x, zq.y);
+#pragma unroll
+    for (int n = 0; n < NB; ++n) unit32_at<kMorse>(t, dx, dy, dxy2, add2(hz[n], naz), kCoul, sm[n]);
+}
+
+template <int NB>
+__device__ __forceinline__ void add_strip(const Sum2 (&sm)[NB], Acc (&acc)[NB]) {
+#pragma unroll
+    for (int n = 0; n < NB; ++n) {
+        const float v[4] = {-(sm[n].gx.x + sm[n].gx.y), -(sm[n].gy.x + sm[n].gy.y),
+                            -(sm[n].gz.x + sm[n].gz.y), sm[n].e.x + sm[n].e.y};
+        acc[n].add(v);
+    }
+}
+
+// Coulomb on or off is a compile-time choice, full chunks run without bounds
+// tests and the last, partial chunk with them.
+template <bool kMorse, bool kCoul, int NB>
 __device__ __forceinline__ void sum_units_strip(const TermPair32* units, int begin, int end,
                                                 float2 hx, float2 hy, const float2 (&hz)[NB],
-                                                bool coul, Acc (&acc)[NB]) {
+                                                Acc (&acc)[NB]) {
     constexpr int kUnits = kChunk / 2;
-    for (int u0 = begin; u0 < end; u0 += kUnits) {
+    int u0 = begin;
+    for (; u0 + kUnits <= end; u0 += kUnits) {
         Sum2 sm[NB];
 #pragma unroll
         for (int n = 0; n < NB; ++n) sm[n].gx = sm[n].gy = sm[n].gz = sm[n].e = f2(0.f);
 #pragma unroll
-        for (int c = 0; c < kUnits; ++c) {
-            if (u0 + c < end) {
-                const TermPair32& t = units[u0 + c];
-                const float4 xy = t.xy, zq = t.zq;
-                const float2 dx = add2(hx, make_float2(xy.x, xy.y));
-                const float2 dy = add2(hy, make_float2(xy.z, xy.w));
-                const float2 dxy2 = fma2(dy, dy, mul2(dx, dx));
-                const float2 naz = make_float2(zq.x, zq.y);
+        for (int c = 0; c < kUnits; ++c) unit32_strip<kMorse, kCoul, NB>(units[u0 + c], hx, hy, hz, sm);
+        add_strip<NB>(sm, acc);
+    }
+    if (u0 < end) {
+        Sum2 sm[NB];
 #pragma unroll
-                for (int n = 0; n < NB; ++n)
-                    unit32_at<kMorse>(t, dx, dy, dxy2, add2(hz[n], naz), coul, sm[n]);
-            }
-        }
+        for (int n = 0; n < NB; ++n) sm[n].gx = sm[n].gy = sm[n].gz = sm[n].e = f2(0.f);
 #pragma unroll
-        for (int n = 0; n < NB; ++n) {
-            const float v[4] = {-(sm[n].gx.x + sm[n].gx.y), -(sm[n].gy.x + sm[n].gy.y),
-                                -(sm[n].gz.x + sm[n].gz.y), sm[n].e.x + sm[n].e.y};
-            acc[n].add(v);
-        }
+        for (int c = 0; c < kUnits - 1; ++c)
+            if (u0 + c < end) unit32_strip<kMorse, kCoul, NB>(units[u0 + c], hx, hy, hz, sm);
+        add_strip<NB>(sm, acc);
     }
 }
 
@@ -781,8 +800,13 @@ __global__ void __launch_bounds__(256) relax32_kernel(const BatchScan* __restric
             tp.hx = f2(g.ex.hi);
             tp.hy = f2(g.ey.hi);
             tp.hz = f2(g.ez.hi);
-            sum_units<G, false>(units, 0, n_units_lj, lg, tp, coul, acc);
-            sum_units<G, true>(units, n_units_lj, n_units, lg, tp, coul, acc);
+            if (coul) {
+                sum_units<G, false, true>(units, 0, n_units_lj, lg, tp, acc);
+                sum_units<G, true, true>(units, n_units_lj, n_units, lg, tp, acc);
+            } else {
+                sum_units<G, false, false>(units, 0, n_units_lj, lg, tp, acc);
+                sum_units<G, true, false>(units, n_units_lj, n_units, lg, tp, acc);
+            }
         }
         if (G > 1) acc.template group_reduce<G>();
 
@@ -1097,8 +1121,13 @@ __global__ void __launch_bounds__(256, 2) grid_build32_kernel(const ScanParams p
             for (int q = threadIdx.x; q < cnt; q += blockDim.x) tile[q] = p.units32[t0 + q];
             __syncthreads();
             const int lj_end = min(max(n_lj - t0, 0), cnt);
-            sum_units_strip<false, kStrip>(tile, 0, lj_end, hx, hy, hz, coul, acc);
-            sum_units_strip<true, kStrip>(tile, lj_end, cnt, hx, hy, hz, coul, acc);
+            if (coul) {
+                sum_units_strip<false, true, kStrip>(tile, 0, lj_end, hx, hy, hz, acc);
+                sum_units_strip<true, true, kStrip>(tile, lj_end, cnt, hx, hy, hz, acc);
+            } else {
+                sum_units_strip<false, false, kStrip>(tile, 0, lj_end, hx, hy, hz, acc);
+                sum_units_strip<true, false, kStrip>(tile, lj_end, cnt, hx, hy, hz, acc);
+            }
         }
         if (valid) {
 #pragma unroll

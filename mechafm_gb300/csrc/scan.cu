@@ -627,13 +627,16 @@ void check_device_errors(const RunCounters& c) {
 }
 
 // Default FP32 launch shape: enough lanes per column that every SM gets work
-// several times over; one column per tile, so that a group takes its next
-// column from the shared queue when it frees up and the queue (in descending
-// expected cost) stays shared until the last columns: longer tiles reserve
-// columns for a warp's lanes early and leave the end of a launch statically
-// assigned (measured on the 401 x 401 cluster at G = 1: 100 ms at one column
-// per tile, 114 ms at 32).
-Relax32Config default_config(long long n_cols, int max_terms, const mafm_run_opts* o) {
+// several times over.  One scan: one column per tile, so that a group takes
+// its next column from the shared queue when it frees up and the queue (in
+// descending expected cost) stays shared until the last columns; longer tiles
+// reserve columns for a warp's lanes early and leave the end of a launch
+// statically assigned (401 x 401 cluster at G = 1: 100 ms at one column per
+// tile, 114 ms at 32).  Several scans: one column per group per tile, because
+// a warp whose next tile belongs to another scan first waits for all its
+// groups, and with one-column tiles nearly every warp would wait at every
+// scan boundary (256 scans: 2.3x slower).
+Relax32Config default_config(long long n_cols, int max_terms, const mafm_run_opts* o, int n_scans) {
     Relax32Config c{};
     c.block = (o && o->block_threads) ? o->block_threads : 256;
     const long long lanes_cap = (long long)sm_count() * 512;
@@ -641,7 +644,7 @@ Relax32Config default_config(long long n_cols, int max_terms, const mafm_run_opt
     while (G < 32 && n_cols * G < 4 * lanes_cap) G *= 2;
     if (max_terms <= 1) G = 1;
     c.lanes = (o && o->lanes_per_column) ? o->lanes_per_column : G;
-    c.cols_per_tile = (o && o->columns_per_tile) ? o->columns_per_tile : 1;
+    c.cols_per_tile = (o && o->columns_per_tile) ? o->columns_per_tile : (n_scans > 1 ? 32 / c.lanes : 1);
     // Shared slice per warp, in 32 B term slots: the paired records of up to
     // 400 terms (each kind's run padded to even: + 2); 12.9 KB per warp keeps
     // two 8-warp blocks per SM.
@@ -788,7 +791,7 @@ int mafm_run(mafm_scan* scan, const mafm_run_opts* opts, mafm_point* out, mafm_r
                 b.order = scan->order.p;
             }
             write_batch<<<1, 1, 0, st>>>(scan->batch.p, b);
-            const Relax32Config cfg = default_config(ce - cb, b.p.n_terms_direct, opts);
+            const Relax32Config cfg = default_config(ce - cb, b.p.n_terms_direct, opts, 1);
             const long long n_tiles = ((long long)(ce - cb) + cfg.cols_per_tile - 1) / cfg.cols_per_tile;
             cuda_check(launch_relax32(scan->batch.p, 1, n_tiles, cfg, scan->ctr.p, st), "relax32 launch");
         }
@@ -848,7 +851,7 @@ int mafm_run_batch(mafm_scan* const* scans, int32_t n_scans, const mafm_run_opts
             ensure_order(*s, st);
             max_terms = std::max(max_terms, s->d.rigidgrid ? 0 : s->P.n_terms);
         }
-        Relax32Config cfg = default_config(total_cols, max_terms, opts);
+        Relax32Config cfg = default_config(total_cols, max_terms, opts, n_scans);
         long long tiles = 0;
         // host outputs: pinned ones are written directly, pageable ones staged
         std::vector<mafm_point*> pinned((size_t)n_scans, nullptr);
@@ -996,8 +999,8 @@ BatchScan scan_batch_entry(const mafm_scan* s, mafm_point* out) {
     return b;
 }
 
-Relax32Config relax32_config(long long n_cols, int max_terms, const mafm_run_opts* o) {
-    return default_config(n_cols, max_terms, o);
+Relax32Config relax32_config(long long n_cols, int max_terms, const mafm_run_opts* o, int n_scans) {
+    return default_config(n_cols, max_terms, o, n_scans);
 }
 
 void check_run_errors(const RunCounters& c) { check_device_errors(c); }
@@ -1053,7 +1056,7 @@ void plan_build(mafm_plan& p, mafm_scan* const* scans, int n, const mafm_run_opt
         cols += (long long)scans[i]->d.nx * scans[i]->d.ny;
         max_terms = std::max(max_terms, scan_direct_terms(scans[i]));
     }
-    p.cfg = default_config(cols, max_terms, opts);
+    p.cfg = default_config(cols, max_terms, opts, n);
     std::vector<BatchScan> bs = batch_entries(scans, n, outs, p.cfg, p.tiles);
     p.n_scans = n;
     p.list.alloc(bs.size());
@@ -1134,8 +1137,9 @@ int mafm_plan_config(const mafm_plan* plan, mafm_run_opts* opts) {
 }
 
 // Time launch shapes on the scans themselves and keep the fastest: lanes per
-// column first (block 256, one column per tile), then block size and tile
-// length around the best lane count.
+// column first (block 256; tiles of 1 and 32 / G columns, 32 / G only for
+// batches), then block size and tile length (1, 4, 32 / G and 128 / G
+// columns) around the best lane count.
 int mafm_autotune(mafm_scan* const* scans, int32_t n_scans, mafm_run_opts* best, double* best_ms,
                   void* stream) {
     return guarded([&] {
@@ -1184,13 +1188,24 @@ int mafm_autotune(mafm_scan* const* scans, int32_t n_scans, mafm_run_opts* best,
         for (int G : lane_set) {
             if (G > 1 && G > std::max(max_terms, 1)) break;
             o.lanes_per_column = G;
-            o.columns_per_tile = 1;
-            const double ms = time_opts(o);
-            if (ms < keep_ms) { keep_ms = ms; keep = o; }
+            // one-column tiles balance large scans; whole-warp tiles keep a
+            // warp's lanes busy when there are fewer columns than groups
+            for (int tile : {1, 32 / G}) {
+                if (n_scans > 1 && tile == 1) continue;
+                o.columns_per_tile = tile;
+                const double ms = time_opts(o);
+                if (ms < keep_ms) { keep_ms = ms; keep = o; }
+            }
         }
         mafm_run_opts base = keep;
         for (int block : {128, 256}) {
-            for (int tile : {1, 4}) {
+            const int G = base.lanes_per_column;
+            int tiles[4] = {1, 4, 32 / G, 128 / G};
+            for (int ti = 0; ti < 4; ++ti) {
+                const int tile = tiles[ti];
+                bool seen = false;
+                for (int tj = 0; tj < ti; ++tj) seen |= tiles[tj] == tile;
+                if (seen) continue;
                 mafm_run_opts c = base;
                 c.block_threads = block;
                 c.columns_per_tile = tile;
