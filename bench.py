@@ -54,11 +54,16 @@ L2_FLUSH_BYTES = 512 << 20
 FLOPS_LJ, FLOPS_MORSE, FLOPS_COUL = 25, 29, 20
 # Algorithmic bytes of one trilinear lookup: 8 FP32 {F, E} nodes.
 BYTES_LOOKUP = 8 * 16
+# DRAM bytes per trilinear lookup of the rigid-grid relax: ncu dram__bytes
+# (20.13 GB/s x 17.454 ms = 351.3 MB) over the 190,890,530 lookups of one
+# 200 x 200 px slab launch: the grid nodes read once and the output records
+# written (gathers within a column are served by L1 and L2).
+DRAM_BYTES_PER_LOOKUP = 351.3e6 / 190890530
 # DRAM bytes (read + write) per relaxed point of relax32_kernel, from one ncu
-# capture of the cluster at 285 x 285 px x 41 z (173.2 MB for 3,330,225
+# capture of the cluster at 285 x 285 px x 41 z (171.9 MB for 3,330,225
 # points); the traffic is the 64 B output record per point, so it scales with
 # the points.
-DRAM_BYTES_PER_POINT = 173.2e6 / 3330225
+DRAM_BYTES_PER_POINT = 171.9e6 / 3330225
 CPU_TARGET_S = 10.0        # CPU sample length
 RIGID_CROP = 16            # pixels per side of the rigid-grid CPU sample
 FP64_RIGID_CROP = 64       # pixels per side of the rigid-grid FP64 comparison
@@ -690,11 +695,15 @@ def ours(args, rank, world, local):
         else:
             hp, src = hbm_peak()
             gbs = st.force_evals * BYTES_LOOKUP / (ms_relax / 1000.0) / 1e9
-            relax_line = {"bound": "hbm", "achieved": gbs, "peak": hp, "unit": "GB/s",
-                          "frac": gbs / hp, "traffic": None, "peak_source": src,
+            relax_line = {"bound": "gather latency (L1-resident), not HBM", "achieved": gbs,
+                          "peak": hp, "unit": "GB/s", "frac": gbs / hp,
+                          "traffic": DRAM_BYTES_PER_LOOKUP * st.force_evals, "peak_source": src,
+                          "traffic_source": "ncu dram__bytes of one 200x200 px slab launch "
+                                            "(190.9 M lookups), scaled by lookups",
                           "kernel": "relax32_kernel (trilinear lookups)", "kernel_ms": ms_relax,
                           "bytes_per_lookup": BYTES_LOOKUP, "lookups": int(st.force_evals),
-                          "note": "algorithmic bytes of the gathers; most are served by L2"}
+                          "note": "achieved = algorithmic bytes of the gathers; ncu: L1 hit 91 %, "
+                                  "L2 hit 83 % at 3 % L2 throughput, DRAM 20 GB/s, issue 43 %"}
         rooflines = [(ms_relax, relax_line)]
         if rigid:
             nodes = sum(rigid_nodes(s.desc.c) for s in rigid)
@@ -730,8 +739,11 @@ def ours(args, rank, world, local):
                        "launch": {"lanes_per_column": used.lanes_per_column,
                                   "block_threads": used.block_threads,
                                   "columns_per_tile": used.columns_per_tile,
-                                  "chosen_by": "autotuner" if tune_ms is not None else "default",
-                                  "column_order": "expected cost, descending",
+                                  "chosen_by": ("autotuner" if tune_ms is not None else
+                                                "forced" if (args.lanes or args.block or args.tile)
+                                                else "default"),
+                                  "column_order": ("natural (rigid grid: no pair terms to cost)"
+                                                   if rigid else "expected cost, descending"),
                                   "cuda_graph": True},
                        "l2": f"{L2_FLUSH_BYTES >> 20} MiB buffer written between timed steps",
                        "fire_steps_per_step": int(st.total_steps),

@@ -173,7 +173,7 @@ struct Sum2 {
 // (:29-40), plus Coulomb (:42-51) when `coul`.  1/r comes from rsqrt.approx
 // and LJ's 1/r^2 is its square, which Coulomb reuses (qq/r^3 = (qq/r)/r^2).
 // Accumulates -F and E into s.
-template <bool kMorse>
+template <bool kMorse, bool kDeriveLJ>
 __device__ __forceinline__ void unit32_at(const TermPair32& t, float2 dx, float2 dy, float2 dxy2,
                                           float2 dz, bool coul, Sum2& s) {
     const float4 zq = t.zq, pa = t.pa, pb = t.pb;
@@ -181,11 +181,22 @@ __device__ __forceinline__ void unit32_at(const TermPair32& t, float2 dx, float2
     const float2 ir = make_float2(rsqrt_fast(r2.x), rsqrt_fast(r2.y));
     float2 nfs, e;
     if (!kMorse) {
-        // E = r^-6 (es12 r^-6 - es6), -F/d = r^-8 (6 es6 - 12 es12 r^-6)
         const float2 ir2 = mul2(ir, ir);
         const float2 ir6 = mul2(mul2(ir2, ir2), ir2);
-        e = mul2(ir6, fma2(make_float2(pa.z, pa.w), ir6, make_float2(pa.x, pa.y)));
-        nfs = mul2(mul2(ir6, ir2), fma2(make_float2(pb.x, pb.y), ir6, make_float2(pb.z, pb.w)));
+        if (kDeriveLJ) {
+            // A = es12 r^-6, t = A - es6: E = r^-6 t, -F/d = -6 r^-8 (A + t);
+            // the record's fourth float4 is not read (one shared load fewer
+            // per record for two multiplies: the relax loop is limited by
+            // shared loads as much as by the FMA pipe)
+            const float2 A = mul2(make_float2(pa.z, pa.w), ir6);
+            const float2 tt = add2(A, make_float2(pa.x, pa.y));
+            e = mul2(ir6, tt);
+            nfs = mul2(mul2(ir6, ir2), mul2(add2(A, tt), f2(-6.f)));
+        } else {
+            // E = r^-6 (es12 r^-6 - es6), -F/d = r^-8 (6 es6 - 12 es12 r^-6)
+            e = mul2(ir6, fma2(make_float2(pa.z, pa.w), ir6, make_float2(pa.x, pa.y)));
+            nfs = mul2(mul2(ir6, ir2), fma2(make_float2(pb.x, pb.y), ir6, make_float2(pb.z, pb.w)));
+        }
         if (coul) {
             const float2 nec = mul2(make_float2(zq.z, zq.w), ir);          // -qq/r
             nfs = fma2(nec, ir2, nfs);
@@ -217,7 +228,7 @@ __device__ __forceinline__ void unit32(const TermPair32& t, const Tip2& p, bool 
     const float2 dx = add2(p.hx, make_float2(xy.x, xy.y));   // tip - atom
     const float2 dy = add2(p.hy, make_float2(xy.z, xy.w));
     const float2 dz = add2(p.hz, make_float2(zq.x, zq.y));
-    unit32_at<kMorse>(t, dx, dy, fma2(dy, dy, mul2(dx, dx)), dz, coul, s);
+    unit32_at<kMorse, true>(t, dx, dy, fma2(dy, dy, mul2(dx, dx)), dz, coul, s);
 }
 
 // Units [begin, end) of one kind: lane lg of the group takes begin + lg,
@@ -263,7 +274,8 @@ __device__ __forceinline__ void unit32_strip(const TermPair32& t, float2 hx, flo
     const float2 dxy2 = fma2(dy, dy, mul2(dx, dx));
     const float2 naz = make_float2(zq.x, zq.y);
 #pragma unroll
-    for (int n = 0; n < NB; ++n) unit32_at<kMorse>(t, dx, dy, dxy2, add2(hz[n], naz), kCoul, sm[n]);
+    for (int n = 0; n < NB; ++n)
+        unit32_at<kMorse, false>(t, dx, dy, dxy2, add2(hz[n], naz), kCoul, sm[n]);
 }
 
 template <int NB>
