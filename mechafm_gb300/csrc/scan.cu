@@ -626,25 +626,34 @@ void check_device_errors(const RunCounters& c) {
         fail(MAFM_E_DEVICE, "the relax kernel stopped at its watchdog time limit");
 }
 
-// Default FP32 launch shape: enough lanes per column that every SM gets work
-// several times over.  One scan: one column per tile, so that a group takes
-// its next column from the shared queue when it frees up and the queue (in
-// descending expected cost) stays shared until the last columns; longer tiles
-// reserve columns for a warp's lanes early and leave the end of a launch
-// statically assigned (401 x 401 cluster at G = 1: 100 ms at one column per
-// tile, 114 ms at 32).  Several scans: one column per group per tile, because
-// a warp whose next tile belongs to another scan first waits for all its
-// groups, and with one-column tiles nearly every warp would wait at every
-// scan boundary (256 scans: 2.3x slower).
+// Default FP32 launch shape (the autotuner's measurements behind it: 401 x 401
+// cluster, 101 x 101 graphene, 128 x 128 cluster, 256-scan batch).
+// Lanes per column: the fewest that give a quarter of the resident lanes a
+// column each; one lane per column does the least work per term, and small
+// scans gain from a few lanes more, but not from filling every lane (101 x
+// 101: G = 2 in 26.9 ms, G = 8 in 47 ms).
+// Tile: one column when the scan has at least twice as many columns as there
+// are groups, so that a group takes its next column from the shared queue
+// when it frees up and the queue (in descending expected cost) stays shared
+// until the last columns; longer tiles reserve columns for a warp's lanes
+// early and leave the end of a launch statically assigned (401 x 401 at G =
+// 1: 100 ms at one column per tile, 114 ms at 32).  Otherwise one column per
+// group: spreading few columns over every warp lowers the active lanes per
+// issued instruction (101 x 101 at G = 2: 43.1 ms at one column per tile,
+// 26.9 ms at 16).  Several scans: one column per group, because a warp whose
+// next tile belongs to another scan first waits for all its groups, and with
+// one-column tiles nearly every warp would wait at every scan boundary (256
+// scans: 2.3x slower).
 Relax32Config default_config(long long n_cols, int max_terms, const mafm_run_opts* o, int n_scans) {
     Relax32Config c{};
     c.block = (o && o->block_threads) ? o->block_threads : 256;
-    const long long lanes_cap = (long long)sm_count() * 512;
+    const long long lanes_cap = (long long)sm_count() * 512;   // two 256-thread blocks per SM
     int G = 1;
-    while (G < 32 && n_cols * G < 4 * lanes_cap) G *= 2;
+    while (G < 32 && n_cols * G < lanes_cap / 4) G *= 2;
     if (max_terms <= 1) G = 1;
     c.lanes = (o && o->lanes_per_column) ? o->lanes_per_column : G;
-    c.cols_per_tile = (o && o->columns_per_tile) ? o->columns_per_tile : (n_scans > 1 ? 32 / c.lanes : 1);
+    const bool long_queue = n_scans <= 1 && n_cols >= 2 * (lanes_cap / c.lanes);
+    c.cols_per_tile = (o && o->columns_per_tile) ? o->columns_per_tile : (long_queue ? 1 : 32 / c.lanes);
     // Shared slice per warp, in 32 B term slots: the paired records of up to
     // 400 terms (each kind's run padded to even: + 2); 12.9 KB per warp keeps
     // two 8-warp blocks per SM.
