@@ -146,9 +146,12 @@ typedef struct mafm_point {
 
 typedef struct mafm_run_opts {
     int32_t precision;          /* MAFM_FP64 or MAFM_FP32C */
-    int32_t lanes_per_column;   /* FP32C: 1,2,4,8,16,32 lanes share a column; 0 = tuned */
-    int32_t block_threads;      /* 0 = default */
-    int32_t columns_per_tile;   /* FP32C: warp work-tile size in columns; 0 = default */
+    int32_t lanes_per_column;   /* FP32C: 1,2,4,8,16,32 lanes share a column; 0 = default
+                                   (from the column count; mafm_autotune measures) */
+    int32_t block_threads;      /* 0 = default (256) */
+    int32_t columns_per_tile;   /* FP32C: columns a warp takes from the shared queue at a
+                                   time; 0 = default (1 for a large single scan, else one
+                                   or four per group) */
     int32_t col_begin;          /* relax only columns [col_begin, col_end) of */
     int32_t col_end;            /*   i*ny + j; 0,0 = all */
 } mafm_run_opts;

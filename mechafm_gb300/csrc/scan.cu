@@ -640,10 +640,11 @@ void check_device_errors(const RunCounters& c) {
 // 1: 100 ms at one column per tile, 114 ms at 32).  Otherwise one column per
 // group: spreading few columns over every warp lowers the active lanes per
 // issued instruction (101 x 101 at G = 2: 43.1 ms at one column per tile,
-// 26.9 ms at 16).  Several scans: one column per group, because a warp whose
-// next tile belongs to another scan first waits for all its groups, and with
-// one-column tiles nearly every warp would wait at every scan boundary (256
-// scans: 2.3x slower).
+// 26.9 ms at 16).  Several scans: four columns per group, because a warp
+// whose next tile belongs to another scan first waits for all its groups:
+// with one-column tiles nearly every warp would wait at every scan boundary
+// (256 scans: 2.3x slower), and longer tiles make those waits rarer (256
+// scans at G = 2: 64-column tiles fastest).
 Relax32Config default_config(long long n_cols, int max_terms, const mafm_run_opts* o, int n_scans) {
     Relax32Config c{};
     c.block = (o && o->block_threads) ? o->block_threads : 256;
@@ -653,7 +654,8 @@ Relax32Config default_config(long long n_cols, int max_terms, const mafm_run_opt
     if (max_terms <= 1) G = 1;
     c.lanes = (o && o->lanes_per_column) ? o->lanes_per_column : G;
     const bool long_queue = n_scans <= 1 && n_cols >= 2 * (lanes_cap / c.lanes);
-    c.cols_per_tile = (o && o->columns_per_tile) ? o->columns_per_tile : (long_queue ? 1 : 32 / c.lanes);
+    const int tile = n_scans > 1 ? 128 / c.lanes : long_queue ? 1 : 32 / c.lanes;
+    c.cols_per_tile = (o && o->columns_per_tile) ? o->columns_per_tile : tile;
     // Shared slice per warp, in 32 B term slots: the paired records of up to
     // 400 terms (each kind's run padded to even: + 2); 12.9 KB per warp keeps
     // two 8-warp blocks per SM.
