@@ -154,6 +154,26 @@ def test_batch_equals_single_runs():
     assert stats.total_steps == sum(int(s["steps"].sum()) for s in singles)
 
 
+@pytest.mark.parametrize("name", ["cluster_ef", "graphene_pbc", "slab_es"])
+def test_fp32c_column_does_not_depend_on_its_launch(name):
+    """A column's FP32C result is the same bits whether it is relaxed alone or
+    inside a full launch, at any tile length: columns go to warps from a
+    shared queue in an order that varies from run to run, so nothing of a
+    column's arithmetic may depend on which lanes or neighbours it gets."""
+    desc = Input(golden(name).input).desc()
+    scan = Scan(desc, device=0)
+    nz = desc.c.nz
+    n = desc.n_columns
+    for lanes, tile in ((1, 1), (1, 32), (2, 1), (8, 4)):
+        full, _ = scan.run(_abi.FP32C, lanes=lanes, tile=tile)
+        for c in sorted({0, 7 % n, n // 2, n - 1}):
+            one, _ = scan.run(_abi.FP32C, lanes=lanes, tile=tile, col_begin=c, col_end=c + 1)
+            want = full[c * nz:(c + 1) * nz]
+            for f in ("tip", "force", "energy", "steps", "status"):
+                np.testing.assert_array_equal(one[f], want[f], err_msg=f"lanes {lanes} tile {tile} column {c} {f}")
+    scan.close()
+
+
 def test_column_ranges_compose():
     case = golden("graphene_pbc")
     desc = Input(case.input).desc()
