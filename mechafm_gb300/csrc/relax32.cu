@@ -32,6 +32,12 @@ namespace {
 
 constexpr unsigned kFull = 0xffffffffu;
 constexpr int kChunk = 8;                 // terms summed plainly before a compensated add
+// Records (term pairs) per compensated add in the grid build: a node sums
+// thousands of terms (18,432 on the periodic slab), most of them small; 64
+// terms per plain FP32 sum keep the grid's accuracy (tip within 1e-3 A on the
+// same fraction of points as 8 terms per sum) and take the compensation from
+// a quarter of the FMA-pipe work to a few percent (slab build 1504 -> 1326 ms).
+constexpr int kBuildChunkUnits = 32;
 constexpr long long kWaitLimit = 1ll << 24;  // bounded mbarrier wait (iterations)
 
 enum : int { PH_EVAL0 = 0, PH_EVAL1 = 1, PH_EVAL2 = 2, PH_EVAL3 = 3, PH_OUT = 4 };
@@ -288,28 +294,37 @@ __device__ __forceinline__ void add_strip(const Sum2 (&sm)[NB], Acc (&acc)[NB]) 
     }
 }
 
-// Coulomb on or off is a compile-time choice, full chunks run without bounds
-// tests and the last, partial chunk with them.
-template <bool kMorse, bool kCoul, int NB>
+// Coulomb on or off is a compile-time choice.  kU records (2 kU terms) are
+// summed plainly per compensated add, four at a time; full chunks run
+// without bounds tests and the last, partial chunk with them.
+template <bool kMorse, bool kCoul, int NB, int kU>
 __device__ __forceinline__ void sum_units_strip(const TermPair32* units, int begin, int end,
                                                 float2 hx, float2 hy, const float2 (&hz)[NB],
                                                 Acc (&acc)[NB]) {
-    constexpr int kUnits = kChunk / 2;
+    static_assert(kU % 4 == 0, "records per chunk: a multiple of 4");
     int u0 = begin;
-    for (; u0 + kUnits <= end; u0 += kUnits) {
+    for (; u0 + kU <= end; u0 += kU) {
         Sum2 sm[NB];
 #pragma unroll
         for (int n = 0; n < NB; ++n) sm[n].gx = sm[n].gy = sm[n].gz = sm[n].e = f2(0.f);
+#pragma unroll 1
+        for (int h = 0; h < kU; h += 4) {
 #pragma unroll
-        for (int c = 0; c < kUnits; ++c) unit32_strip<kMorse, kCoul, NB>(units[u0 + c], hx, hy, hz, sm);
+            for (int c = 0; c < 4; ++c) unit32_strip<kMorse, kCoul, NB>(units[u0 + h + c], hx, hy, hz, sm);
+        }
         add_strip<NB>(sm, acc);
     }
     if (u0 < end) {
         Sum2 sm[NB];
 #pragma unroll
         for (int n = 0; n < NB; ++n) sm[n].gx = sm[n].gy = sm[n].gz = sm[n].e = f2(0.f);
+#pragma unroll 1
+        for (; u0 + 4 <= end; u0 += 4) {
 #pragma unroll
-        for (int c = 0; c < kUnits - 1; ++c)
+            for (int c = 0; c < 4; ++c) unit32_strip<kMorse, kCoul, NB>(units[u0 + c], hx, hy, hz, sm);
+        }
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
             if (u0 + c < end) unit32_strip<kMorse, kCoul, NB>(units[u0 + c], hx, hy, hz, sm);
         add_strip<NB>(sm, acc);
     }
@@ -1134,11 +1149,11 @@ __global__ void __launch_bounds__(256, 2) grid_build32_kernel(const ScanParams p
             __syncthreads();
             const int lj_end = min(max(n_lj - t0, 0), cnt);
             if (coul) {
-                sum_units_strip<false, true, kStrip>(tile, 0, lj_end, hx, hy, hz, acc);
-                sum_units_strip<true, true, kStrip>(tile, lj_end, cnt, hx, hy, hz, acc);
+                sum_units_strip<false, true, kStrip, kBuildChunkUnits>(tile, 0, lj_end, hx, hy, hz, acc);
+                sum_units_strip<true, true, kStrip, kBuildChunkUnits>(tile, lj_end, cnt, hx, hy, hz, acc);
             } else {
-                sum_units_strip<false, false, kStrip>(tile, 0, lj_end, hx, hy, hz, acc);
-                sum_units_strip<true, false, kStrip>(tile, lj_end, cnt, hx, hy, hz, acc);
+                sum_units_strip<false, false, kStrip, kBuildChunkUnits>(tile, 0, lj_end, hx, hy, hz, acc);
+                sum_units_strip<true, false, kStrip, kBuildChunkUnits>(tile, lj_end, cnt, hx, hy, hz, acc);
             }
         }
         if (valid) {
