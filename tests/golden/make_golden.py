@@ -86,6 +86,21 @@ def cases():
     c.append(("graphene_ovwrt", ow, (50, 53, 20, 23), None))
     c.append(("cluster_maxsteps", synth.cluster_60(zlow=9.0, maxsteps="40"),
               (180, 183, 180, 183), None))
+    # kJ/mol units (qbase 1389.354563, parse.cpp:286-288), the molecule centred
+    # away from the scan centre (center, system.cpp:119-136) and an XY spring
+    # with a non-zero rest length (harm k r0, interactions.cpp:252-266)
+    kj = synth.cluster_60(zlow=8.0, units="kJ/mol", center="1.5 -2.0")
+    kj.harm = (0.5, 0.3)
+    c.append(("cluster_kj_r0", kj, (190, 193, 205, 208), None))
+    # surface normal along y or x: the file's axes are rotated into z
+    # (rotateCoordAxes "ZXY" / "YZX", system.cpp:68-89), so the graphene is
+    # written with (y, z, x) resp. (z, x, y) as its file coordinates
+    gy = synth.graphene_72(zlow=8.0, surface_normal="y")
+    gy.pos = gy.pos[:, [1, 2, 0]].copy()
+    c.append(("graphene_normal_y", gy, (45, 48, 45, 48), None))
+    gx = synth.graphene_72(zlow=8.0, surface_normal="x")
+    gx.pos = gx.pos[:, [2, 0, 1]].copy()
+    c.append(("graphene_normal_x", gx, (45, 48, 45, 48), None))
     # flexible molecule (bonds, angles, dihedrals, non-bonded pairs between
     # fragments, substrate, XY tethers); the middle column's atom states too
     c.append(("flex_naph", synth.flexible_naphthalene(), (0, 3, 0, 3), "states"))

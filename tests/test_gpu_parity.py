@@ -28,7 +28,7 @@ from mechafm_gb300.scan import Input, Scan, run_batch
 pytestmark = pytest.mark.gpu
 
 EXACT_CASES = {"graphene_ef", "graphene_euler", "graphene_sd", "graphene_pbc", "graphene_grid",
-               "graphene_ovwrt"}
+               "graphene_ovwrt", "graphene_normal_x", "graphene_normal_y"}
 TIP_TOL = 1e-3
 FZ_TOL = 1e-3
 FZ_FLOOR = 0.01
