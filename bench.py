@@ -515,13 +515,14 @@ def ours(args, rank, world, local):
         torch.cuda.synchronize()
         t_grid = time.perf_counter() - t0
 
-    # launch shape: the autotuner (on at most 32 scans of a batch)
+    # launch shape: the autotuner (its sweep on the first 32 scans of a batch,
+    # then the winner against the default shape on all of them)
     opts = _abi.RunOpts(_abi.FP32C, args.lanes, args.block, args.tile, 0, 0)
     tune_ms = None
     if not args.no_tune and not (args.lanes or args.block or args.tile):
         best = _abi.RunOpts()
         tms = C.c_double()
-        _abi.check(L.mafm_autotune(handles, min(n, 32), C.byref(best), C.byref(tms), sptr))
+        _abi.check(L.mafm_autotune(handles, n, C.byref(best), C.byref(tms), sptr))
         opts, tune_ms = best, tms.value
     plan = C.c_void_p()
     _abi.check(L.mafm_plan_create(handles, n, C.byref(opts), optrs, C.byref(plan)))

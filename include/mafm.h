@@ -304,7 +304,9 @@ int mafm_plan_destroy(mafm_plan* plan);
 
 /* Autotuner: times launch shapes of the FP32C kernel (lanes per column, block
  * size, columns per warp tile) on the given scans and returns the fastest in
- * best (pass it to mafm_run / mafm_run_batch / mafm_plan_create).  No
+ * best (pass it to mafm_run / mafm_run_batch / mafm_plan_create).  For a batch
+ * of more than 32 scans the sweep runs on the first 32 and its winner is timed
+ * against the default shape on the whole batch.  No
  * counterpart in the reference, whose OpenMP schedule is fixed (dynamic, 1,
  * simulation.cpp:78). */
 int mafm_autotune(mafm_scan* const* scans, int32_t n_scans, mafm_run_opts* best, double* best_ms,

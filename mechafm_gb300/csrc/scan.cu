@@ -1148,9 +1148,9 @@ int mafm_plan_config(const mafm_plan* plan, mafm_run_opts* opts) {
 }
 
 // Time launch shapes on the scans themselves and keep the fastest: lanes per
-// column first (block 256; tiles of 1 and 32 / G columns, 32 / G only for
-// batches), then block size and tile length (1, 4, 32 / G and 128 / G
-// columns) around the best lane count.
+// column first (block 256; tiles of 1 and 32 / G columns for one scan, 32 / G
+// and 128 / G for batches), then block size and tile length (1, 4, 32 / G and
+// 128 / G columns) around the best lane count.
 int mafm_autotune(mafm_scan* const* scans, int32_t n_scans, mafm_run_opts* best, double* best_ms,
                   void* stream) {
     return guarded([&] {
@@ -1176,10 +1176,17 @@ int mafm_autotune(mafm_scan* const* scans, int32_t n_scans, mafm_run_opts* best,
         cuda_check(cudaEventCreate(&e0), "cudaEventCreate");
         cuda_check(cudaEventCreate(&e1), "cudaEventCreate");
         struct EvGuard { cudaEvent_t a, b; ~EvGuard() { cudaEventDestroy(a); cudaEventDestroy(b); } } eg{e0, e1};
-        auto time_opts = [&](const mafm_run_opts& o) {
+        // The sweep runs on the first kTrialScans scans of a batch; the winner
+        // is then timed against the default shape on the whole batch (a
+        // subset of a large batch can favour another shape: 256 molecules,
+        // the first 32 favour G = 2 with 64-column tiles, all 256 G = 1 with
+        // 128-column tiles, 5 % faster).
+        constexpr int kTrialScans = 32;
+        int n_time = std::min(n_scans, (int32_t)kTrialScans);
+        auto time_opts = [&](const mafm_run_opts& o, bool warm = true) {
             mafm_plan p;
-            plan_build(p, scans, n_scans, &o, outs.data(), st);
-            plan_launch(p, st);   // warm-up: module load, attributes
+            plan_build(p, scans, n_time, &o, outs.data(), st);
+            if (warm) plan_launch(p, st);   // warm-up: module load, attributes
             cuda_check(cudaEventRecord(e0, st), "cudaEventRecord");
             plan_launch(p, st);
             cuda_check(cudaEventRecord(e1, st), "cudaEventRecord");
@@ -1199,10 +1206,12 @@ int mafm_autotune(mafm_scan* const* scans, int32_t n_scans, mafm_run_opts* best,
         for (int G : lane_set) {
             if (G > 1 && G > std::max(max_terms, 1)) break;
             o.lanes_per_column = G;
-            // one-column tiles balance large scans; whole-warp tiles keep a
-            // warp's lanes busy when there are fewer columns than groups
-            for (int tile : {1, 32 / G}) {
-                if (n_scans > 1 && tile == 1) continue;
+            // one scan: one-column tiles balance large scans, whole-warp tiles
+            // keep a warp's lanes busy when there are fewer columns than
+            // groups; batches: one or four columns per group (longer tiles
+            // make the waits at scan boundaries rarer)
+            const int t_a = n_scans > 1 ? 32 / G : 1, t_b = n_scans > 1 ? 128 / G : 32 / G;
+            for (int tile : {t_a, t_b}) {
                 o.columns_per_tile = tile;
                 const double ms = time_opts(o);
                 if (ms < keep_ms) { keep_ms = ms; keep = o; }
@@ -1223,6 +1232,22 @@ int mafm_autotune(mafm_scan* const* scans, int32_t n_scans, mafm_run_opts* best,
                 if (block == base.block_threads && c.columns_per_tile == base.columns_per_tile) continue;
                 const double ms = time_opts(c);
                 if (ms < keep_ms) { keep_ms = ms; keep = c; }
+            }
+        }
+        if (n_scans > n_time) {
+            n_time = n_scans;
+            mafm_run_opts def{};
+            def.precision = MAFM_FP32C;
+            const double ms_keep = time_opts(keep, false), ms_def = time_opts(def, false);
+            keep_ms = ms_keep;
+            if (ms_def < ms_keep) {
+                mafm_plan p;
+                plan_build(p, scans, n_scans, &def, outs.data(), st);
+                keep = def;
+                keep.lanes_per_column = p.cfg.lanes;
+                keep.block_threads = p.cfg.block;
+                keep.columns_per_tile = p.cfg.cols_per_tile;
+                keep_ms = ms_def;
             }
         }
         *best = keep;
