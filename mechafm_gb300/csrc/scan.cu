@@ -1211,8 +1211,8 @@ int mafm_autotune(mafm_scan* const* scans, int32_t n_scans, mafm_run_opts* best,
             // groups; batches: one or four columns per group (longer tiles
             // make the waits at scan boundaries rarer)
             const int t_a = n_scans > 1 ? 32 / G : 1, t_b = n_scans > 1 ? 128 / G : 32 / G;
-            for (int tile : {t_a, t_b}) {
-                o.columns_per_tile = tile;
+            for (int ti = 0; ti < (t_b == t_a ? 1 : 2); ++ti) {   // G = 32: one shape
+                o.columns_per_tile = ti == 0 ? t_a : t_b;
                 const double ms = time_opts(o);
                 if (ms < keep_ms) { keep_ms = ms; keep = o; }
             }
