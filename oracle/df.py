@@ -2,8 +2,11 @@
 
 numpy restatement of the reference's frequency-shift post-processing
 (simple-vafm-image.py), used only by tests/ to check libmafm's mafm_df and
-mafm_df_adjoint.  The script is Python 2 with matplotlib and file globbing,
-so it does not run here; this follows its arithmetic line by line:
+mafm_df_adjoint.  The script is Python 2 with matplotlib and file globbing;
+this follows its arithmetic line by line, and is pinned to the script's own
+results (tests/golden/df_script, made by running the script under Python 3
+with its plotting stubbed on scan files written by the reference
+executable): weights and images bit for bit.
 
 * weights: simple-vafm-image.py:77-89 (Giessibl, Beilstein J. Nanotechnol.
   3:238, 2012) — fshiftfac, the ampcut precaution (Python float % and //),
