@@ -26,6 +26,10 @@ set-up, grid build and relaxation are timed apart and scaled to the full scan.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
                   [--workload NAME]
+  profiling knobs: --pixels P (a smaller scan), --lanes/--block/--tile
+  (a forced launch shape instead of the autotuner), --no-tune (the default
+  shape), --sweep (times lanes x block x tile shapes, to stderr),
+  --no-fp64 and --cpu-seconds 0 (skip the comparison legs).
 """
 from __future__ import annotations
 
