@@ -3,7 +3,7 @@
 // Persistent, multi-scan relaxation kernel.  Work is a list of tiles of pixel
 // columns, possibly from many scans (a batch); each warp takes one tile at a
 // time with an atomic counter, and G lanes share one column (G = 1..32, a
-// launch parameter picked by the autotuner).  The warp's current scan's
+// launch parameter from the autotuner or the default rule in scan.cu).  The warp's current scan's
 // tip–atom terms are staged into the warp's slice of shared memory with a
 // bulk copy (cp.async.bulk + mbarrier); every lane of a group sums its share
 // of the terms, then the group combines its sums with xor shuffles.
@@ -14,11 +14,15 @@
 // produces a point's output (System::getOutput, system.cpp:28-51) is one more
 // slot, so lanes never wait on a divergent extra pair loop.
 //
-// Precision: pair terms in FP32 (fast reciprocal refined by one Newton step,
-// fast rsqrt/exp); tip positions in double-float (hi + lo FP32) so that
-// tip–atom separations keep ~1e-7 relative accuracy; per-lane sums compensated
-// (two-sum over chunks of terms); the energy behind the e/ef convergence test
-// and the tip–dummy XY spring are FP64.
+// Precision: pair terms in FP32, two per packed f32x2 instruction in the relax
+// loop (1/r from rsqrt.approx, LJ's 1/r^2 its square, exp from __expf); the
+// scalar paths (tip–dummy term, sampling) take 1/r^2 from rcp.approx refined
+// by one Newton step.  Tip positions, the energy behind the e/ef convergence
+// test and the spring energy are double-floats (hi + lo FP32), so that
+// tip–atom separations keep ~1e-7 relative accuracy without FP64 arithmetic
+// in the slot path; sums are compensated (Kahan) over chunks of 8 terms in
+// the relax loop and 64 in the grid build, and groups combine them with
+// two-sums.
 //
 // Reference correspondence (src/): as relax64.cu — interactions.cpp:15-51,
 // 244-266; force_grid.cpp:88-275; integrators.cpp:8-111; minimiser.cpp:15-129;
