@@ -70,6 +70,14 @@ CASES = [
     ("no_xyz", SCAN, dict(drop=["xyzfile"]), "Specify at least an xyzfile!", _abi.MAFM_E_PARSE),
     ("no_par", SCAN, dict(drop=["paramfile"]), "Specify at least a parameter file!", _abi.MAFM_E_PARSE),
     ("no_tip", SCAN, dict(drop=["tipatom"]), "Specify at least a tip atom!", _abi.MAFM_E_PARSE),
+    ("no_dummy", SCAN, dict(drop=["dummyatom"]), "Specify at least a dummy atom!", _abi.MAFM_E_PARSE),
+    ("onoff", SCAN, dict(replace={"coulomb": "coulomb maybe"}), "Option coulomb must be either on or off!",
+     _abi.MAFM_E_PARSE),
+    ("ext_flex", SCAN, dict(replace={"coulomb": "coulomb off", "flexible": "flexible on"},
+                            add=["use_external_potential on", "e_potential_file x.cube"]),
+     "External potential can be used only for non-flexible systems!", _abi.MAFM_E_PARSE),
+    ("flex_bond", SCAN, dict(replace={"flexible": "flexible on"}),
+     "No harmonic bond parameters found in parameter file!", _abi.MAFM_E_PARSE),
     ("no_minterm", SCAN, dict(drop=["minterm"]),
      "Specify at least a minimization termination criterion (e, f, or ef)!", _abi.MAFM_E_PARSE),
     ("grid_flex", SCAN, dict(add=["rigidgrid on", "flexible on"]),
@@ -115,10 +123,20 @@ def test_missing_files(tmp_path):
     with pytest.raises(_abi.MafmError) as e:
         Input(str(tmp_path / "nope.scan"))
     assert e.value.code == _abi.MAFM_E_IO and "does not exist" in e.value.msg
+    os.remove(tmp_path / PAR)
+    with pytest.raises(_abi.MafmError) as e:
+        Input(inp)
+    assert e.value.msg == f"No parameter file {tmp_path}/{PAR} found!"
+    ref = reference_error(inp)
+    if ref is not None:
+        assert ref == e.value.msg
     os.remove(tmp_path / XYZ)
     with pytest.raises(_abi.MafmError) as e:
         Input(inp)
     assert e.value.msg == f"No such file: {tmp_path}/{XYZ}!"
+    ref = reference_error(inp)
+    if ref is not None:
+        assert ref == e.value.msg
 
 
 def test_xyz_formats_and_charge_source(tmp_path):
