@@ -99,9 +99,20 @@ int main(int argc, char* argv[]) {
         pretty("Done!");
     }
 
-    // Simulation::run (simulation.cpp:67-143): the x rows in ten chunks, with
-    // the reference's progress lines.
+    // Simulation::run (simulation.cpp:67-143): the x rows in ten chunks; after
+    // each, the reference's progress test (simulation.cpp:132-137: the float
+    // fraction of pixels done against thresholds stepped by 0.1 in double),
+    // so the same ten lines are printed whatever the number of rows.
     pretty("Starting simulation");
+    const double report_interval = 0.1;
+    double next_report = report_interval;
+    auto report = [&](int pixels_done) {
+        const double progress = 1.0f * pixels_done / (d.nx * d.ny);
+        while (progress >= next_report) {
+            pretty("Finished %4.1f %% of the simulation", 100 * next_report);
+            next_report += report_interval;
+        }
+    };
     std::vector<mafm_point> pts((size_t)n_total);
     uint64_t total_steps = 0;
     const int chunks = 10;
@@ -126,7 +137,7 @@ int main(int argc, char* argv[]) {
             check(mafm_run(scan, &o, pts.data() + (size_t)cb * d.nz, &st, nullptr));
         }
         total_steps += st.total_steps;
-        pretty("Finished %4.1f %% of the simulation", 100.0 * i1 / d.nx);
+        report(ce);
     }
     check(mafm_write_output(in, pts.data(), outdir.c_str(), gzip));
     if (scan) check(mafm_scan_destroy(scan));

@@ -131,6 +131,13 @@ def cli_cases():
     ]
 
 
+def mask_times(text: str) -> str:
+    """Stdout of the executable with the numbers of its two timing lines
+    (mechafm.cpp:140-152) replaced by '#'."""
+    import re
+    return re.sub(r"(wall time is|simulation took) [0-9.]+ seconds", r"\1 # seconds", text)
+
+
 def make_cli_fixture(name, spec):
     """Sorted rows of every scan-*.dat file, and statistics.txt without its timing lines."""
     folder = os.path.join(HERE, name)
@@ -138,8 +145,13 @@ def make_cli_fixture(name, spec):
         shutil.rmtree(folder)
     inp = spec.write(folder)
     out = os.path.join(folder, "_out")
-    subprocess.run([oracle.REF_CLI, os.path.abspath(inp), out], check=True, cwd=folder,
-                   stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+    r = subprocess.run([oracle.REF_CLI, os.path.abspath(inp), out], check=True, cwd=folder,
+                       capture_output=True, text=True)
+    # the executable's stdout with the two run times masked and the fixture
+    # and output folders as {DIR} and {OUT}
+    text = mask_times(r.stdout).replace(out, "{OUT}").replace(folder, "{DIR}")
+    with open(os.path.join(folder, "cli_stdout.txt"), "w") as f:
+        f.write(text)
     rows = []
     for fn in sorted(os.listdir(out)):
         if fn.startswith("scan-"):

@@ -34,3 +34,32 @@ def test_cli_argument_errors(cid, args, message, tmp_path):
         assert ref.returncode == r.returncode
         assert ref.stdout == r.stdout
         assert ref.stderr == r.stderr
+
+
+def _placeholders(text, folder, out):
+    return text.replace(out, "{OUT}").replace(folder, "{DIR}")
+
+
+def cli_stdout(name, tmp_path):
+    """(our stdout lines with {DIR}/{OUT} placeholders, the reference's, exit code)."""
+    from conftest import GOLDEN, MANIFEST
+    folder = os.path.join(GOLDEN, name)
+    out = str(tmp_path / "out")
+    r = _run(build.CLI, [os.path.join(folder, MANIFEST[name]["input"]), out], folder)
+    ours = _placeholders(r.stdout, folder, out).splitlines()
+    with open(os.path.join(folder, "cli_stdout.txt")) as f:
+        ref = f.read().splitlines()
+    return ours, ref, r.returncode
+
+
+@pytest.mark.parametrize("name", ["cli_cluster", "cli_pbc", "cli_flex"])
+def test_cli_banner_and_settings_match_reference(name, tmp_path):
+    """Everything the executable prints before the relaxation starts (banner,
+    the echo of every input setting, the 3D data grid) equals the reference
+    executable's stdout (tests/golden/cli_*/cli_stdout.txt).  Without a GPU
+    the run stops right after these lines."""
+    if not os.path.exists(build.CLI):
+        pytest.skip("mechafm-gpu not built")
+    ours, ref, _ = cli_stdout(name, tmp_path)
+    k = ref.index("+- Starting simulation")
+    assert ours[:k] == ref[:k]

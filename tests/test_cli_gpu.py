@@ -77,3 +77,42 @@ def test_cli_flexible_state_files(tmp_path):
         else:
             assert gt == wt
     assert "+- Wrote" in stdout
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", CASES)
+def test_cli_stdout_matches_reference_executable(name, tmp_path):
+    """The whole stdout against the reference executable's: the same lines
+    before the relaxation and after it (run times masked, step totals to
+    1 %), the same state
+    files reported, and the reference's progress lines a prefix of ours (its
+    pixel counter is shared by OpenMP threads without synchronisation, so it
+    can stop short of 100 %; ours prints all ten)."""
+    import re
+    from test_cli_args import cli_stdout
+    ours, ref, rc = cli_stdout(name, tmp_path)
+    assert rc == 0
+    ours = [re.sub(r"(wall time is|simulation took) [0-9.]+ seconds", r"\1 # seconds", l) for l in ours]
+    k, e = ref.index("+- Starting simulation"), ref.index("+- Simulation run finished")
+    ko, eo = ours.index("+- Starting simulation"), ours.index("+- Simulation run finished")
+    assert ours[:k + 1] == ref[:k + 1]
+    # the step totals: FP64 kernels agree with the reference to rounding, so
+    # a FIRE decision may flip on a near-tie (1 %); every other line exactly
+    tail, tail_ref = ours[eo:], ref[e:]
+    assert len(tail) == len(tail_ref)
+    for a, b in zip(tail, tail_ref):
+        if "minimization steps" in a:
+            na, nb = float(re.findall(r"[0-9.]+", a)[0]), float(re.findall(r"[0-9.]+", b)[0])
+            assert re.sub(r"[0-9.]+", "#", a) == re.sub(r"[0-9.]+", "#", b)
+            assert abs(na - nb) <= 0.01 * nb, (a, b)
+        else:
+            assert a == b
+    mid, mid_ref = ours[ko + 1:eo], ref[k + 1:e]
+    wrote = sorted(l for l in mid if l.startswith("+- Wrote"))
+    assert wrote == sorted(l for l in mid_ref if l.startswith("+- Wrote"))
+    fin = [l for l in mid if l.startswith("+- Finished")]
+    fin_ref = [l for l in mid_ref if l.startswith("+- Finished")]
+    assert fin == ["+- Finished %4.1f %% of the simulation" % (10.0 * (i + 1)) for i in range(10)]
+    assert fin[:len(fin_ref)] == fin_ref
+    assert len(mid) == len(wrote) + len(fin)
+
