@@ -1,0 +1,79 @@
+"""Seeded random scans run through the reference's own code (oracle/_ref,
+built here from the reference sources) and through the oracle and the
+product's front-end: every relaxed point bit for bit, and the prepared
+system (positions, charges, offset, grid, tip-dummy distance) identical.
+
+Each case draws a planar molecule (12-40 atoms of C/N/O/H, random charges)
+and a random combination of the options on the path: integrator (euler,
+midpoint, rk4), minimiser (FIRE, SD), termination (e, f, ef), Coulomb,
+units, tip-dummy Coulomb, a pair_ovwrt line (LJ or Morse), the XY spring's
+rest length, maxsteps.  Skipped where the reference is not built (the GPU
+host)."""
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+from mechafm_gb300 import synth
+from mechafm_gb300.scan import Input
+
+pytestmark = pytest.mark.skipif(not oracle.ref_available(), reason="reference not built here")
+
+N_CASES = 16
+
+
+def random_spec(seed):
+    rng = np.random.default_rng(1000 + seed)
+    n = int(rng.integers(12, 41))
+    types, pos, q = synth.planar_molecule(n, rng)
+    minimiser = str(rng.choice(["FIRE", "FIRE", "SD"]))
+    opt = dict(
+        integrator=str(rng.choice(["euler", "midpoint", "rk4"])),
+        minimiser=minimiser,
+        minterm=str(rng.choice(["e", "f", "ef"])),
+        coulomb=str(rng.choice(["on", "off"])),
+        units=str(rng.choice(["kcal/mol", "kJ/mol", "eV"])),
+        dt="0.01" if minimiser == "SD" else str(rng.choice(["0.001", "0.002"])),
+        maxsteps=str(rng.choice(["5000", "5000", "60"])),
+        area="0.6 0.6", dx="0.3", dy="0.3", zhigh="10.0", zlow="9.6", dz="0.1",
+    )
+    if opt["coulomb"] == "on" and rng.random() < 0.5:
+        opt["tip_dummy_coulomb"] = "on"
+    o = synth.base_options(**opt)
+    over = []
+    pick = rng.random()
+    if pick < 0.35:
+        over.append(("C", "O", "lj", float(rng.uniform(0.05, 0.2)), float(rng.uniform(3.0, 3.6))))
+    elif pick < 0.7:
+        over.append(("N", "O", "morse", float(rng.uniform(0.05, 0.15)),
+                     float(rng.uniform(1.2, 1.8)), float(rng.uniform(3.0, 3.4))))
+    harm = (float(rng.uniform(0.3, 0.8)), float(rng.choice([0.0, 0.0, rng.uniform(0.05, 0.4)])))
+    return synth.ScanInput(f"rand{seed}", types, pos, q, dict(synth.CLUSTER_PARAMS), over, harm, o)
+
+
+@pytest.mark.parametrize("seed", range(N_CASES))
+def test_oracle_matches_reference_on_random_scans(seed, tmp_path):
+    spec = random_spec(seed)
+    inp = spec.write(str(tmp_path))
+    rec = oracle.ref_scan(inp, str(tmp_path / "ref.bin"))
+    rec = rec[np.lexsort((rec[:, 2], rec[:, 1], rec[:, 0]))]
+    desc = Input(inp).desc()
+    pts, _ = oracle.run(desc)
+    assert len(pts) == len(rec)
+    np.testing.assert_array_equal(pts["steps"], rec[:, 3].astype(np.int32))
+    np.testing.assert_array_equal(pts["tip"], rec[:, 4:7])
+    np.testing.assert_array_equal(pts["force"], rec[:, 13:16])
+    np.testing.assert_array_equal(pts["energy"], rec[:, 16])
+
+    sysinfo = oracle.ref_system(inp, str(tmp_path / "sys.txt"))
+    atoms = desc.atoms()
+    d = desc.c
+    np.testing.assert_array_equal(atoms["pos"], np.array([a[1:4] for a in sysinfo["atoms"]])[2:])
+    np.testing.assert_array_equal(np.array(d.offset[:]), np.array(sysinfo["offset"]))
+    assert [d.nx, d.ny, d.nz] == list(sysinfo["n_points"])
+    assert d.tip_dummy_d == float(sysinfo["tip_dummy_d"])
+    if d.coulomb:
+        ch = np.array([a[4] for a in sysinfo["atoms"]])
+        np.testing.assert_array_equal(atoms["charge"], ch[2:])
+        assert d.tip_charge == ch[1]
