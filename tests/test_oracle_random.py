@@ -7,8 +7,9 @@ Each case draws a planar molecule (12-40 atoms of C/N/O/H, random charges)
 and a random combination of the options on the path: integrator (euler,
 midpoint, rk4), minimiser (FIRE, SD), termination (e, f, ef), Coulomb,
 units, tip-dummy Coulomb, a pair_ovwrt line (LJ or Morse), the XY spring's
-rest length, maxsteps.  Skipped where the reference is not built (the GPU
-host)."""
+rest length, maxsteps; and jittered graphene sheets under in-plane periodic
+images, over pair terms or a rigid force grid.  Skipped where the reference
+is not built (the GPU host)."""
 import os
 
 import numpy as np
@@ -52,9 +53,37 @@ def random_spec(seed):
     return synth.ScanInput(f"rand{seed}", types, pos, q, dict(synth.CLUSTER_PARAMS), over, harm, o)
 
 
+def random_periodic_spec(seed):
+    """A jittered graphene sheet under in-plane periodic images (vdw_pbc),
+    over pair terms or a rigid force grid."""
+    rng = np.random.default_rng(2000 + seed)
+    a = 1.42 * np.sqrt(3.0)
+    cell_a, cell_b = (6 * a, 0.0, 0.0), (3 * a, 3 * a * np.sqrt(3.0), 0.0)
+    minimiser = str(rng.choice(["FIRE", "FIRE", "SD"]))
+    spec = synth.graphene_72(
+        area=float(rng.choice([1.0, 2.0])), step=0.5, zhigh=10.0, zlow=9.6, dz=0.1,
+        vdw_pbc="on", rigidgrid=str(rng.choice(["on", "off"])),
+        integrator=str(rng.choice(["euler", "midpoint", "rk4"])), minimiser=minimiser,
+        minterm=str(rng.choice(["e", "f", "ef"])),
+        dt="0.01" if minimiser == "SD" else "0.001",
+        cell_a=" ".join(repr(float(x)) for x in cell_a),
+        cell_b=" ".join(repr(float(x)) for x in cell_b), cell_c="0.0 0.0 20.0")
+    spec.pos = spec.pos + rng.normal(scale=0.05, size=spec.pos.shape)
+    spec.harm = (float(rng.uniform(0.3, 0.8)), float(rng.choice([0.0, 0.2])))
+    return spec
+
+
 @pytest.mark.parametrize("seed", range(N_CASES))
 def test_oracle_matches_reference_on_random_scans(seed, tmp_path):
-    spec = random_spec(seed)
+    check_against_reference(random_spec(seed), tmp_path)
+
+
+@pytest.mark.parametrize("seed", range(8))
+def test_oracle_matches_reference_on_random_periodic_scans(seed, tmp_path):
+    check_against_reference(random_periodic_spec(seed), tmp_path)
+
+
+def check_against_reference(spec, tmp_path):
     inp = spec.write(str(tmp_path))
     rec = oracle.ref_scan(inp, str(tmp_path / "ref.bin"))
     rec = rec[np.lexsort((rec[:, 2], rec[:, 1], rec[:, 0]))]
