@@ -1,0 +1,51 @@
+"""The GPU kernels on the seeded random scans of test_oracle_random (random
+molecules and option combinations; periodic sheets over pair terms or a
+rigid grid), against the oracle, which is pinned to the reference on the
+same scans.  Small scans (45-80 points), so the bars are per case:
+
+  FP64   step counts equal on >= 95 % of the points, the tip within 1e-6 A
+         where they are, within 0.05 A everywhere (FIRE decisions may flip
+         on near-ties where exp or the FFT differ in the last bit);
+  FP32C  step counts equal on >= 80 %; where they are, the tip within
+         1e-3 A and Fz within 1e-3 relative (floor 0.01) on >= 90 %; the tip
+         within 0.05 A everywhere.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from mechafm_gb300 import _abi
+from mechafm_gb300.scan import Input, Scan
+from test_oracle_random import N_CASES, random_periodic_spec, random_spec
+
+pytestmark = pytest.mark.gpu
+
+SPECS = [("mol", s) for s in range(N_CASES)] + [("pbc", s) for s in range(8)]
+
+
+def _spec(kind, seed):
+    return random_spec(seed) if kind == "mol" else random_periodic_spec(seed)
+
+
+@pytest.mark.parametrize("kind,seed", SPECS, ids=[f"{k}{s}" for k, s in SPECS])
+def test_gpu_kernels_match_oracle_on_random_scans(kind, seed, tmp_path):
+    desc = Input(_spec(kind, seed).write(str(tmp_path))).desc()
+    want, _ = oracle.run(desc)
+    scan = Scan(desc, device=0)
+    p64, _ = scan.run(_abi.FP64)
+    p32, _ = scan.run(_abi.FP32C)
+    scan.close()
+
+    same = p64["steps"] == want["steps"]
+    d = np.abs(p64["tip"] - want["tip"]).max(axis=1)
+    assert same.mean() >= 0.95, same.mean()
+    assert d[same].max() <= 1e-6, d[same].max()
+    assert d.max() <= 0.05
+
+    same = p32["steps"] == want["steps"]
+    d = np.abs(p32["tip"] - want["tip"]).max(axis=1)
+    fz = np.abs(p32["force"][:, 2] - want["force"][:, 2]) / np.maximum(np.abs(want["force"][:, 2]), 0.01)
+    assert same.mean() >= 0.8, same.mean()
+    ok = (d <= 1e-3) & (fz <= 1e-3)
+    assert ok[same].mean() >= 0.9, (ok[same].mean(), d.max(), fz.max())
+    assert d.max() <= 0.05
