@@ -106,3 +106,47 @@ def check_against_reference(spec, tmp_path):
         ch = np.array([a[4] for a in sysinfo["atoms"]])
         np.testing.assert_array_equal(atoms["charge"], ch[2:])
         assert d.tip_charge == ch[1]
+
+
+def random_flexible_spec(seed):
+    """Naphthalene plus H2 (flexible): random jitter, fixed / tethered flags,
+    force constants, integrator, minimiser and termination."""
+    rng = np.random.default_rng(3000 + seed)
+    minimiser = str(rng.choice(["FIRE", "FIRE", "SD"]))
+    spec = synth.flexible_naphthalene(
+        seed=100 + seed, zhigh=10.0, zlow=9.6, dz=0.2,
+        integrator=str(rng.choice(["euler", "midpoint", "rk4"])), minimiser=minimiser,
+        minterm=str(rng.choice(["e", "f", "ef"])), dt="0.005" if minimiser == "SD" else "0.001")
+    spec.pos = spec.pos + rng.normal(0.0, 0.03, spec.pos.shape)
+    spec.fixed = rng.choice([0, 0, 0, 0, 1, 2], size=len(spec.types))
+    spec.extra_param_lines = [
+        f"bond {rng.uniform(30.0, 70.0)!r}", f"angle {rng.uniform(10.0, 30.0)!r}",
+        f"dihedral {rng.uniform(1.0, 3.0)!r}", "substrate 0.1 3.0 3.0 7.5 1.0",
+        "topobond C C 1.40", "topobond C H 1.09", "topobond H H 0.74"]
+    return spec
+
+
+@pytest.mark.parametrize("seed", range(8))
+def test_oracle_matches_reference_on_random_flexible_scans(seed, tmp_path):
+    import subprocess
+    spec = random_flexible_spec(seed)
+    inp = spec.write(str(tmp_path))
+    rec = oracle.ref_scan(inp, str(tmp_path / "ref.bin"))
+    rec = rec[np.lexsort((rec[:, 2], rec[:, 1], rec[:, 0]))]
+    src = Input(inp)
+    desc, flex = src.desc(), src.flex_desc()
+    pts, _, _ = oracle.flex_run(desc, flex)
+    np.testing.assert_array_equal(pts["steps"], rec[:, 3].astype(np.int32))
+    np.testing.assert_array_equal(pts["tip"], rec[:, 4:7])
+    np.testing.assert_array_equal(pts["force"], rec[:, 13:16])
+    np.testing.assert_array_equal(pts["energy"], rec[:, 16])
+    # the middle column's atom states (System::makeXYZFile)
+    d = desc.c
+    col = d.nx * d.ny // 2
+    sbin = str(tmp_path / "states.bin")
+    subprocess.run([oracle.REF_DUMP, "states", inp, sbin, str(col // d.ny), str(col % d.ny)],
+                   check=True, cwd=str(tmp_path), stdout=subprocess.DEVNULL,
+                   stderr=subprocess.DEVNULL)
+    want = np.fromfile(sbin).reshape(d.nz, -1, 3)
+    _, _, states = oracle.flex_run(desc, flex, col, col + 1, state_column=col)
+    np.testing.assert_array_equal(states, want)
