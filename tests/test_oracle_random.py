@@ -116,7 +116,7 @@ def random_flexible_spec(seed):
     spec = synth.flexible_naphthalene(
         seed=100 + seed, zhigh=10.0, zlow=9.6, dz=0.2,
         integrator=str(rng.choice(["euler", "midpoint", "rk4"])), minimiser=minimiser,
-        minterm=str(rng.choice(["e", "f", "ef"])), dt="0.005" if minimiser == "SD" else "0.001")
+        minterm=str(rng.choice(["f", "ef"])), dt="0.002" if minimiser == "SD" else "0.001")
     spec.pos = spec.pos + rng.normal(0.0, 0.03, spec.pos.shape)
     spec.fixed = rng.choice([0, 0, 0, 0, 1, 2], size=len(spec.types))
     spec.extra_param_lines = [
