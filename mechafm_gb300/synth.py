@@ -303,7 +303,7 @@ def gaussian_potential(pos: np.ndarray, q: np.ndarray, cell: np.ndarray, n: tupl
     rho_k = np.fft.rfftn(rho)
     with np.errstate(divide="ignore", invalid="ignore"):
         v_k = np.where(K2 > 0, 4 * np.pi * rho_k / K2, 0.0)
-    v = np.fft.irfftn(v_k, s=(n0, n1, n2))
+    v = np.fft.irfftn(v_k, s=(n0, n1, n2), axes=(0, 1, 2))
     return v * BOHR
 
 

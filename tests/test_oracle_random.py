@@ -150,3 +150,48 @@ def test_oracle_matches_reference_on_random_flexible_scans(seed, tmp_path):
     want = np.fromfile(sbin).reshape(d.nz, -1, 3)
     _, _, states = oracle.flex_run(desc, flex, col, col + 1, state_column=col)
     np.testing.assert_array_equal(states, want)
+
+
+def random_field_spec(seed):
+    """A small periodic slab under the FFT-derived external field: random
+    charges, cell shear, voxel size, rigid grid on or off, dummy height."""
+    rng = np.random.default_rng(4000 + seed)
+    vox = int(rng.choice([20, 24, 28]))
+    zlow = float(rng.choice([9.0, 9.3]))
+    return synth.slab(seed=50 + seed, nlx=3, nly=6, layers=2, cell=(6.0, 6.0, 10.0),
+                      cube_n=(vox, vox, vox * 10 // 6), pixels=3, step=0.5,
+                      zhigh=zlow + 0.6, zlow=zlow, dz=0.2, rigidgrid=bool(rng.random() < 0.4),
+                      external=True, shear=float(rng.choice([0.0, 0.0, 0.2])),
+                      tip_charge=float(rng.choice([-0.05, -0.02])),
+                      integrator=str(rng.choice(["euler", "midpoint", "rk4"])),
+                      minterm=str(rng.choice(["f", "ef"])))
+
+
+@pytest.mark.parametrize("seed", range(6))
+def test_oracle_matches_reference_on_random_field_scans(seed, tmp_path):
+    """The external field through a direct DFT (oracle) against kiss_fft
+    (reference): rounding-level differences, so step counts equal on >= 95 %
+    of the points and the tip within 1e-6 A where they are.  Where the
+    reference stops with an error (tip outside the rigid grid, FFT residue),
+    the front end and oracle must stop with the same text."""
+    import subprocess
+    spec = random_field_spec(seed)
+    inp = spec.write(str(tmp_path))
+    r = subprocess.run([oracle.REF_DUMP, "scan", inp, str(tmp_path / "ref.bin")],
+                       cwd=str(tmp_path), capture_output=True, text=True)
+    if r.returncode != 0:
+        msg = [l for l in r.stderr.splitlines() if "what()" in l or "ERROR" in l][-1]
+        msg = msg.split("what():", 1)[-1].split("ERROR (on process 0): ", 1)[-1].strip()
+        from mechafm_gb300 import _abi
+        with pytest.raises(_abi.MafmError) as e:
+            desc = Input(inp).desc()
+            oracle.run(desc)
+        assert msg.split("Value:")[0].strip() in e.value.msg
+        return
+    rec = np.fromfile(str(tmp_path / "ref.bin")).reshape(-1, 25)
+    rec = rec[np.lexsort((rec[:, 2], rec[:, 1], rec[:, 0]))]
+    pts, _ = oracle.run(Input(inp).desc())
+    same = pts["steps"] == rec[:, 3].astype(np.int32)
+    assert same.mean() >= 0.95, same.mean()
+    d = np.abs(pts["tip"] - rec[:, 4:7]).max(axis=1)
+    assert d[same].max() < 1e-6, d[same].max()
