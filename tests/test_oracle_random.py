@@ -167,8 +167,34 @@ def random_field_spec(seed):
                       minterm=str(rng.choice(["f", "ef"])))
 
 
-@pytest.mark.parametrize("seed", range(6))
-def test_oracle_matches_reference_on_random_field_scans(seed, tmp_path):
+def to_normal_y(spec):
+    """The same slab written for `surface_normal y`: file coordinates (y, z, x)
+    and the cube's axes permuted to match, which the reference rotates back
+    (System::rotateCoordAxes, DataGrid::rotateCoordAxes "ZXY",
+    data_grid.cpp:49-69).  The periodic cell still comes from the unrotated
+    cube file (simulation.cpp:38-52), as the reference does."""
+    import copy
+    s = copy.deepcopy(spec)
+    s.pos = spec.pos[:, [1, 2, 0]].copy()
+    vox = np.asarray(spec.cube["voxel"], dtype=float)
+
+    def perm(v):
+        return np.array([v[1], v[2], v[0]])
+
+    s.cube = {"values": np.ascontiguousarray(spec.cube["values"].transpose(1, 2, 0)),
+              "voxel": np.array([perm(vox[1]), perm(vox[2]), perm(vox[0])]),
+              "origin": (0.0, 0.0, 0.0)}
+    s.options = dict(spec.options)
+    s.options["surface_normal"] = "y"
+    return s
+
+
+FIELD_CASES = [(s, False) for s in range(6)] + [(s, True) for s in range(6)]
+
+
+@pytest.mark.parametrize("seed,normal_y", FIELD_CASES,
+                         ids=[f"{s}{'_normal_y' if y else ''}" for s, y in FIELD_CASES])
+def test_oracle_matches_reference_on_random_field_scans(seed, normal_y, tmp_path):
     """The external field through a direct DFT (oracle) against kiss_fft
     (reference): rounding-level differences, so step counts equal on >= 95 %
     of the points and the tip within 1e-6 A where they are.  Where the
@@ -176,6 +202,8 @@ def test_oracle_matches_reference_on_random_field_scans(seed, tmp_path):
     the front end and oracle must stop with the same text."""
     import subprocess
     spec = random_field_spec(seed)
+    if normal_y:
+        spec = to_normal_y(spec)
     inp = spec.write(str(tmp_path))
     r = subprocess.run([oracle.REF_DUMP, "scan", inp, str(tmp_path / "ref.bin")],
                        cwd=str(tmp_path), capture_output=True, text=True)
