@@ -106,6 +106,7 @@ static double len3(v3 v) { return sqrt(v.x * v.x + v.y * v.y + v.z * v.z); }
 
 /* ---- pair terms --------------------------------------------------------- */
 /* r = tip - (atom + shift); the image shift is already in the term position. */
+/* LJInteraction::eval interactions.cpp:15-27, MorseInteraction::eval :29-40. */
 static void term_vdw(const Term* t, v3 tip, v3* f, double* e) {
     v3 r = {tip.x - t->x, tip.y - t->y, tip.z - t->z};
     if (t->kind == MAFM_PAIR_LJ) { /* interactions.cpp:15-27 */
@@ -133,6 +134,7 @@ static void term_coul(double qq, v3 r, v3* f, double* e) { /* interactions.cpp:4
 }
 
 /* ---- trilinear grid lookup, force_grid.cpp:88-275 ----------------------- */
+/* ForceGrid::getGridPointIndex force_grid.cpp:223-249 with pbcGridPoint :252-275. */
 static int grid_index(Ctx* c, const Grid* g, int x, int y, int z) {
     if (x < 0 || y < 0 || z < 0 || x >= g->n[0] || y >= g->n[1] || z >= g->n[2]) {
         if (g->periodic) {
@@ -150,6 +152,7 @@ static int grid_index(Ctx* c, const Grid* g, int x, int y, int z) {
     return (x * g->n[1] + y) * g->n[2] + z;
 }
 
+/* ForceGrid::interpolate force_grid.cpp:88-155, getGridPoint :158-220. */
 static void grid_interp(Ctx* c, const Grid* g, v3 pos, v3* f, double* e, int* outside) {
     int gp[3];
     v3 q = {pos.x - g->origin[0], pos.y - g->origin[1], pos.z - g->origin[2]};
@@ -189,6 +192,9 @@ static void grid_interp(Ctx* c, const Grid* g, v3 pos, v3* f, double* e, int* ou
 
 /* ---- force evaluations --------------------------------------------------- */
 /* Tip–surface terms (the interactions with isTipSurface(), system.cpp:41-51). */
+/* The tip-surface terms in the reference's interaction order
+ * (buildTipSurfaceInteractions simulation.cpp:297-320; GridInteraction
+ * interactions.cpp:244-250; ElectrostaticPotentialInteraction :236-242). */
 static void eval_ts(Ctx* c, v3 tip, v3* F, double* E, int* outside) {
     v3 f = {0, 0, 0};
     double e = 0;
@@ -251,6 +257,7 @@ static void eval_all(Ctx* c, v3 tip, v3 dum, v3* F, double* E, int* outside) {
 }
 
 /* ---- minimisers ---------------------------------------------------------- */
+/* checkConvergence minimiser.cpp:15-37. */
 static int converged(const mafm_scan_desc* d, v3 F, double ediff) {
     switch (d->minterm) {
         case MAFM_TERM_E: return fabs(ediff) < d->etol;
@@ -265,6 +272,8 @@ typedef struct {
     int outside;
 } State;
 
+/* FIREMinimisation minimiser.cpp:67-129 with eulerStep / midpointStep /
+ * rk4Step integrators.cpp:8-21 / 23-54 / 56-111. */
 static int fire(Ctx* c, State* s) {
     const mafm_scan_desc* d = c->d;
     const int n_min = 5;
@@ -346,6 +355,7 @@ static int fire(Ctx* c, State* s) {
     return n_tot;
 }
 
+/* SDMinimisation minimiser.cpp:39-65. */
 static int steepest(Ctx* c, State* s) {
     const mafm_scan_desc* d = c->d;
     int n = 1;
@@ -362,6 +372,7 @@ static int steepest(Ctx* c, State* s) {
 }
 
 /* System::setDummyXY (system.cpp:139-162) */
+/* System::setDummyXY system.cpp:139-162 (PBC wrap relative to the offset). */
 static void dummy_xy(Ctx* c, int wrap, double x, double y, double* ox, double* oy) {
     if (wrap) {
         const mafm_scan_desc* d = c->d;
@@ -379,6 +390,8 @@ static void dummy_xy(Ctx* c, int wrap, double x, double y, double* ox, double* o
 }
 
 /* One pixel column: the loop body of Simulation::run (simulation.cpp:93-122). */
+/* One pixel column of Simulation::run simulation.cpp:93-122: the z descent with
+ * System::lowerTip (system.hpp:51-54) and getOutput (system.cpp:28-51). */
 static void column(Ctx* c, int col, mafm_point* out) {
     const mafm_scan_desc* d = c->d;
     const int i = col / d->ny, j = col % d->ny;
@@ -410,6 +423,8 @@ static void column(Ctx* c, int col, mafm_point* out) {
 }
 
 /* ---- 3-D DFT (definition of kiss_fftnd's transform, no normalisation) ---- */
+/* One axis of the unnormalised 3-D DFT that fft_data_grid / ffti_data_grid
+ * (fft.cpp:11-94) compute with kiss_fftnd. */
 static void dft_axis(double* re, double* im, const int n[3], int axis, int inverse) {
     const int L = n[axis];
     const size_t stride = axis == 0 ? (size_t)n[1] * n[2] : (axis == 1 ? (size_t)n[2] : 1);
@@ -460,6 +475,8 @@ static void dft3(double* re, double* im, const int n[3], int inverse) {
 }
 
 /* ElectrostaticPotentialInteraction ctor, interactions.cpp:53-234. */
+/* ElectrostaticPotentialInteraction ctor interactions.cpp:53-234 and the
+ * potential set-up of Simulation::buildTipSurfaceInteractions simulation.cpp:322-417. */
 static int build_es(Ctx* c) {
     const mafm_scan_desc* d = c->d;
     Grid* g = &c->es;
@@ -569,6 +586,7 @@ static int build_es(Ctx* c) {
 }
 
 /* Simulation::buildTipGridInteractions, simulation.cpp:420-501. */
+/* Simulation::buildTipGridInteractions simulation.cpp:420-501. */
 static void build_grid(Ctx* c) {
     const mafm_scan_desc* d = c->d;
     Grid* g = &c->grid;
@@ -608,6 +626,8 @@ static void build_grid(Ctx* c) {
     c->mode = saved;
 }
 
+/* The interactions of Simulation::buildInteractions simulation.cpp:201-216
+ * (tip-surface :297-417, tip grid :420-501, tip-dummy :503-515). */
 static int ctx_init(Ctx* c, const mafm_scan_desc* d) {
     memset(c, 0, sizeof *c);
     c->d = d;
@@ -660,8 +680,9 @@ static void ctx_free(Ctx* c) {
 
 /* ---- entry points (ctypes) ----------------------------------------------- */
 
-/* Relax columns [col_begin, col_end); out[(col - col_begin)*nz + k].
- * nthreads <= 0 keeps the OpenMP default. */
+/* Relax columns [col_begin, col_end); out[(col - col_begin)*nz + k]
+ * (Simulation::run simulation.cpp:67-143, OpenMP over columns as the
+ * reference's schedule(dynamic, 1)).  nthreads <= 0 keeps the OpenMP default. */
 int oracle_run(const mafm_scan_desc* d, int col_begin, int col_end, mafm_point* out,
                int nthreads, uint64_t* total_steps) {
     Ctx c;
@@ -702,7 +723,9 @@ int oracle_run_split(const mafm_scan_desc* d, int col_begin, int col_end, mafm_p
     return 0;
 }
 
-/* Tip–surface F,E at tip positions; what 1 = external field only. */
+/* Tip–surface F,E at tip positions (the tip-surface sum of System::getOutput,
+ * system.cpp:28-51); what 1 = external field only
+ * (ElectrostaticPotentialInteraction::eval interactions.cpp:236-242). */
 int oracle_sample(const mafm_scan_desc* d, int what, const double* pts, int64_t n, double* out) {
     Ctx c;
     int st = ctx_init(&c, d);
@@ -723,7 +746,8 @@ int oracle_sample(const mafm_scan_desc* d, int what, const double* pts, int64_t 
     return 0;
 }
 
-/* Copy a grid (what 0 = rigid grid, 1 = external field): n, then 4 doubles per node. */
+/* Copy a grid (what 0 = rigid grid of buildTipGridInteractions simulation.cpp:
+ * 420-501, 1 = external field of interactions.cpp:53-234): n, then 4 doubles per node. */
 int oracle_grid(const mafm_scan_desc* d, int what, int32_t n[3], double* out, int64_t cap) {
     Ctx c;
     int st = ctx_init(&c, d);
@@ -743,6 +767,8 @@ int oracle_grid(const mafm_scan_desc* d, int what, int32_t n[3], double* out, in
  * and every term contributes mu . df/dtheta.  The reference itself has no
  * derivatives; this restatement is checked against central finite differences
  * of the oracle's own relaxation in tests/test_adjoint.py. */
+/* Adjoint helpers: derivatives of interactions.cpp:15-51 (no counterpart in the
+ * reference, which has no derivatives). */
 static void pair_s_o(int kind, double p0, double p1, double p2, double r2, double* s, double* dsr) {
     if (kind == MAFM_PAIR_LJ) {
         double ir2 = 1.0 / r2, ir6 = ir2 * ir2 * ir2;
@@ -798,6 +824,9 @@ static void es_jac_o(const Grid* g, v3 pos, double Jg[9]) {
             Jg[3 * m + j] = dFd[m][0] * g->inv[0][j] + dFd[m][1] * g->inv[1][j] + dFd[m][2] * g->inv[2][j];
 }
 
+/* FP64 gradients of sum_p w_p Fz_p by implicit differentiation at each
+ * relaxed point (no counterpart in the reference, which has no derivatives;
+ * pinned by finite differences of the reference's own relaxation). */
 int oracle_adjoint(const mafm_scan_desc* d, const mafm_point* pts, const double* w, double* dpos,
                    double* dcharge, double* dpair) {
     Ctx c;
@@ -955,6 +984,8 @@ static v3 vnorm(v3 a) {
     return z;
 }
 
+/* The flexible-mode interactions: interactions.cpp:15-51 (pairs), :252-266
+ * (tip spring), :268-362 (XY tether, substrate, bond, angle, dihedral). */
 static void fint_eval(const FCtx* c, const FInt* t, const v3* pos, v3* F, double* E) {
     switch (t->type) {
     case FI_LJ: {
@@ -1108,6 +1139,9 @@ static int fl_push(FCtx* c, int* cap, FInt t) {
     return 0;
 }
 
+/* The interaction list of a flexible scan in the reference's order:
+ * buildInteractions simulation.cpp:201-216 with buildSubstrateInteractions
+ * :517-555 and buildSurfaceSurfaceInteractions :557-693. */
 static int fctx_init(FCtx* c, const mafm_scan_desc* d, const mafm_flex_desc* f) {
     memset(c, 0, sizeof *c);
     c->d = d;
@@ -1229,6 +1263,7 @@ typedef struct {
 } FState;
 
 /* one integrator step (integrators.cpp:8-111): forces_/energies_ in F/E */
+/* eulerStep / midpointStep / rk4Step integrators.cpp:8-111 over every free atom. */
 static void fl_step(const FCtx* c, FState* s, double dt) {
     const int n = c->na;
     const mafm_scan_desc* d = c->d;
@@ -1299,6 +1334,7 @@ static int fl_converged(const mafm_scan_desc* d, v3 F, double ediff) {
 }
 
 /* FIREMinimisation / SDMinimisation over all atoms (minimiser.cpp:39-129) */
+/* FIREMinimisation / SDMinimisation minimiser.cpp:39-129 over every free atom. */
 static int fl_minimise(const FCtx* c, FState* s) {
     const mafm_scan_desc* d = c->d;
     const int n = c->na;
@@ -1344,8 +1380,10 @@ static int fl_minimise(const FCtx* c, FState* s) {
     return k;
 }
 
-/* Relax columns [col_begin, col_end) of a flexible scan; states (optional)
- * receives every atom's position after each height of column state_column. */
+/* Relax columns [col_begin, col_end) of a flexible scan (Simulation::run
+ * simulation.cpp:67-143 with flexible on); states (optional) receives every
+ * atom's position after each height of column state_column, as
+ * System::makeXYZFile writes them (system.cpp:54-66, simulation.cpp:114-116). */
 int oracle_flex_run(const mafm_scan_desc* d, const mafm_flex_desc* f, int col_begin, int col_end,
                     mafm_point* out, int nthreads, uint64_t* total_steps, int state_column,
                     double* states) {
