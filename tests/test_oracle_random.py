@@ -7,7 +7,8 @@ Each case draws a planar molecule (12-40 atoms of C/N/O/H, random charges)
 and a random combination of the options on the path: integrator (euler,
 midpoint, rk4), minimiser (FIRE, SD), termination (e, f, ef), Coulomb,
 units, tip-dummy Coulomb, a pair_ovwrt line (LJ or Morse), the XY spring's
-rest length, maxsteps; and jittered graphene sheets under in-plane periodic
+rest length, maxsteps, scan area, steps and centre; and jittered graphene
+sheets under in-plane periodic
 images, over pair terms or a rigid force grid.  Skipped where the reference
 is not built (the GPU host)."""
 import os
@@ -37,8 +38,12 @@ def random_spec(seed):
         units=str(rng.choice(["kcal/mol", "kJ/mol", "eV"])),
         dt="0.01" if minimiser == "SD" else str(rng.choice(["0.001", "0.002"])),
         maxsteps=str(rng.choice(["5000", "5000", "60"])),
-        area="0.6 0.6", dx="0.3", dy="0.3", zhigh="10.0", zlow="9.6", dz="0.1",
+        area=f"{float(rng.choice([0.6, 0.9]))!r} {float(rng.choice([0.4, 0.6]))!r}",
+        dx=repr(float(rng.choice([0.3, 0.2]))), dy=repr(float(rng.choice([0.2, 0.3]))),
+        zhigh="10.0", zlow="9.6", dz=repr(float(rng.choice([0.1, 0.2]))),
     )
+    if rng.random() < 0.5:
+        opt["center"] = f"{rng.uniform(-1.0, 1.0)!r} {rng.uniform(-1.0, 1.0)!r}"
     if opt["coulomb"] == "on" and rng.random() < 0.5:
         opt["tip_dummy_coulomb"] = "on"
     o = synth.base_options(**opt)
