@@ -24,7 +24,7 @@ SPECS = [("mol", s) for s in range(N_CASES)] + [("pbc", s) for s in range(8)]
 
 
 def _spec(kind, seed):
-    return random_spec(seed) if kind == "mol" else random_periodic_spec(seed)
+    return random_spec(seed, geometry=False) if kind == "mol" else random_periodic_spec(seed)
 
 
 @pytest.mark.parametrize("kind,seed", SPECS, ids=[f"{k}{s}" for k, s in SPECS])

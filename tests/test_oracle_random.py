@@ -25,7 +25,9 @@ pytestmark = pytest.mark.skipif(not oracle.ref_available(), reason="reference no
 N_CASES = 16
 
 
-def random_spec(seed):
+def random_spec(seed, geometry=True):
+    """geometry=False keeps a fixed 0.6 x 0.6 A area at 0.3 A steps, dz 0.1
+    (the form the GPU test of these scans was validated on)."""
     rng = np.random.default_rng(1000 + seed)
     n = int(rng.integers(12, 41))
     types, pos, q = synth.planar_molecule(n, rng)
@@ -38,12 +40,15 @@ def random_spec(seed):
         units=str(rng.choice(["kcal/mol", "kJ/mol", "eV"])),
         dt="0.01" if minimiser == "SD" else str(rng.choice(["0.001", "0.002"])),
         maxsteps=str(rng.choice(["5000", "5000", "60"])),
-        area=f"{float(rng.choice([0.6, 0.9]))!r} {float(rng.choice([0.4, 0.6]))!r}",
-        dx=repr(float(rng.choice([0.3, 0.2]))), dy=repr(float(rng.choice([0.2, 0.3]))),
-        zhigh="10.0", zlow="9.6", dz=repr(float(rng.choice([0.1, 0.2]))),
+        area="0.6 0.6", dx="0.3", dy="0.3", zhigh="10.0", zlow="9.6", dz="0.1",
     )
-    if rng.random() < 0.5:
-        opt["center"] = f"{rng.uniform(-1.0, 1.0)!r} {rng.uniform(-1.0, 1.0)!r}"
+    if geometry:
+        g = np.random.default_rng(5000 + seed)
+        opt.update(area=f"{float(g.choice([0.6, 0.9]))!r} {float(g.choice([0.4, 0.6]))!r}",
+                   dx=repr(float(g.choice([0.3, 0.2]))), dy=repr(float(g.choice([0.2, 0.3]))),
+                   dz=repr(float(g.choice([0.1, 0.2]))))
+        if g.random() < 0.5:
+            opt["center"] = f"{g.uniform(-1.0, 1.0)!r} {g.uniform(-1.0, 1.0)!r}"
     if opt["coulomb"] == "on" and rng.random() < 0.5:
         opt["tip_dummy_coulomb"] = "on"
     o = synth.base_options(**opt)
