@@ -280,8 +280,10 @@ int mafm_run_batch(mafm_scan* const* scans, int32_t n_scans, const mafm_run_opts
  *   - All calls share the array and it keeps the last call's contents; each
  *     call clears its counters first.  Calls that overlap on the GPU race:
  *     order them on one stream or with events.
- *   - stats may be NULL; when given, the call synchronises the stream
- *     (kernel_ms is left 0). */
+ *   - The call synchronises the stream and reports device-side failures
+ *     (watchdog, rigid-grid exit, staging timeout) like mafm_run_batch,
+ *     whether or not stats is given; stats may be NULL (kernel_ms is left 0).
+ *   - Outputs must be device memory of the scans' GPU, else MAFM_E_INVALID. */
 #define MAFM_NOALLOC_MAX_SCANS 32
 int mafm_run_batch_noalloc(mafm_scan* const* scans, int32_t n_scans, const mafm_run_opts* opts,
                            mafm_point* const* outs, mafm_run_stats* stats, void* stream);

@@ -581,6 +581,12 @@ __global__ void flex_kernel(FlexKernelArgs A) {
                 S.pos[5] -= P.dz;
             }
             __syncwarp();
+            // the time limit once per height too: a height usually converges in
+            // far fewer than the 1024 steps between the checks above
+            if (__any_sync(0xffffffffu, now_ns() - t0 > A.watchdog_ns)) {
+                err |= ERR_WATCHDOG;
+                break;
+            }
         }
         if (err & ERR_WATCHDOG) break;
     }
@@ -909,8 +915,7 @@ extern "C" int mafm_flex_run(mafm_flex* s, int32_t col_begin, int32_t col_end, m
         A.out = dout;
         A.state_column = state_column;
         A.states = dstates;
-        const char* w = getenv("MAFM_WATCHDOG_S");
-        A.watchdog_ns = (unsigned long long)((w ? atof(w) : 120.0) * 1e9);
+        A.watchdog_ns = watchdog_ns_from_env();
         A.ctr = s->ctr;
         cuda_check(cudaMemsetAsync(s->ctr, 0, sizeof(RunCounters), st), "reset counters");
         const size_t per_warp = (size_t)7 * s->n_sys * 3 * sizeof(double);

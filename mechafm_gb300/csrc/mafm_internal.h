@@ -16,6 +16,7 @@
 #pragma once
 
 #include <cstdint>
+#include <cstdlib>
 #include <new>
 #include <stdexcept>
 #include <string>
@@ -53,6 +54,16 @@ int guarded(F&& f) {
 
 inline void cuda_check(cudaError_t e, const char* what) {
     if (e != cudaSuccess) fail(MAFM_E_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+// Time limit of the persistent relax kernels in nanoseconds: MAFM_WATCHDOG_S
+// seconds (fractions allowed), else 120 s.  Unset, non-numeric, zero,
+// negative or absurdly large values all give the 120 s default.
+inline unsigned long long watchdog_ns_from_env() {
+    const char* w = std::getenv("MAFM_WATCHDOG_S");
+    double s = w ? std::atof(w) : 0.0;
+    if (!(s > 0.0) || s > 1.0e6) s = 120.0;
+    return (unsigned long long)(s * 1.0e9);
 }
 
 // Device error bits (mafm_run_stats.error_word, upper half; lower bits are MAFM_PT_*).
@@ -174,7 +185,7 @@ struct Relax32Config {
     int cols_per_tile;        // columns per warp work tile
     int smem_terms;           // terms staged per warp (larger scans read global memory)
     int blocks;               // 0 = fill the GPU
-    double watchdog_s;        // persistent-kernel time limit (0 = 600 s)
+    unsigned long long watchdog_ns;   // persistent-kernel time limit
 };
 
 cudaError_t launch_relax32(const BatchScan* scans_dev, int n_scans, long long n_tiles,

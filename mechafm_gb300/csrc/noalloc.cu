@@ -63,13 +63,16 @@ __global__ void store_descriptors(BatchScan* dst, DescChunk c) {
     for (int i = 0; i < c.n; ++i) dst[i] = c.b[i];
 }
 
-bool on_device(const void* p) {
+// Device (or managed) memory of the given GPU: the kernel writes the points
+// there directly, so an output on another GPU, or in host memory, is refused.
+bool on_device(const void* p, int device) {
     cudaPointerAttributes a{};
     if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
         cudaGetLastError();
         return false;
     }
-    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+    if (a.type == cudaMemoryTypeManaged) return true;
+    return a.type == cudaMemoryTypeDevice && a.device == device;
 }
 
 }  // namespace
@@ -97,8 +100,9 @@ extern "C" int mafm_run_batch_noalloc(mafm_scan* const* scans, int32_t n_scans,
         for (int i = 0; i < n_scans; ++i) {
             if (!scans[i] || !outs[i]) fail(MAFM_E_INVALID, "null scan or output %d", i);
             if (scan_device(scans[i]) != device) fail(MAFM_E_INVALID, "scans of one call must share a device");
-            if (!on_device(outs[i]))
-                fail(MAFM_E_INVALID, "output %d is not device memory; this entry point copies nothing", i);
+            if (!on_device(outs[i], device))
+                fail(MAFM_E_INVALID, "output %d is not device memory of GPU %d; this entry point "
+                                     "copies nothing", i, device);
             if (!scan_fp32_ready(scans[i]))
                 fail(MAFM_E_INVALID, "scan %d uses a rigid grid whose FP32 copy is not built yet: "
                                      "relax it once with mafm_run (MAFM_FP32C) first", i);
@@ -127,16 +131,19 @@ extern "C" int mafm_run_batch_noalloc(mafm_scan* const* scans, int32_t n_scans,
         cuda_check(cudaGetLastError(), "store descriptors");
         cuda_check(cudaMemsetAsync(ctr, 0, sizeof(RunCounters), st), "clear counters");
         cuda_check(launch_relax32(list, n_scans, tiles, cfg, ctr, st), "relax32 launch");
+        // The counters hold the device error word (watchdog, grid exit, staging
+        // timeout): read them on every call, so that a failed relaxation is
+        // reported whether or not the caller asked for statistics.
+        RunCounters c{};
+        cuda_check(cudaMemcpyAsync(&c, ctr, sizeof c, cudaMemcpyDeviceToHost, st), "read counters");
+        cuda_check(cudaStreamSynchronize(st), "relax");
         if (stats) {
-            RunCounters c{};
-            cuda_check(cudaMemcpyAsync(&c, ctr, sizeof c, cudaMemcpyDeviceToHost, st), "read counters");
-            cuda_check(cudaStreamSynchronize(st), "relax");
             std::memset(stats, 0, sizeof *stats);
             stats->total_steps = c.total_steps;
             stats->force_evals = c.force_evals;
             stats->pair_evals = c.pair_evals;
             stats->error_word = c.error_word;
-            check_run_errors(c);
         }
+        check_run_errors(c);
     });
 }

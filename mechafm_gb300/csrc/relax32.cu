@@ -1199,10 +1199,8 @@ cudaError_t launch_g(const BatchScan* scans, int n_scans, long long n_tiles,
     const long long max_blocks = (warps_needed + cfg.block / 32 - 1) / (cfg.block / 32);
     if (blocks > max_blocks) blocks = (int)max_blocks;
     if (blocks < 1) blocks = 1;
-    const unsigned long long watchdog_ns =
-        (unsigned long long)(cfg.watchdog_s > 0 ? cfg.watchdog_s : 600.0) * 1000000000ull;
     relax32_kernel<G><<<blocks, cfg.block, smem, s>>>(scans, n_scans, n_tiles, cfg.cols_per_tile,
-                                                      cfg.smem_terms, watchdog_ns, ctr);
+                                                      cfg.smem_terms, cfg.watchdog_ns, ctr);
     return cudaGetLastError();
 }
 

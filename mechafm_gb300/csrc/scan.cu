@@ -15,6 +15,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <vector>
@@ -621,7 +622,9 @@ void check_device_errors(const RunCounters& c) {
         fail(MAFM_E_RANGE, "Invalid grid point: the tip left the rigid force grid "
                            "(force_grid.cpp:236-240 stops the reference here)");
     if (c.error_word & ERR_STAGE_TIMEOUT)
-        fail(MAFM_E_DEVICE, "a bounded wait on the term staging barrier expired");
+        fail(MAFM_E_DEVICE, "a bounded wait on the term staging barrier expired; the kernel "
+                            "ended without its results and the device context's state is "
+                            "unspecified (destroy and recreate it)");
     if (c.error_word & ERR_WATCHDOG)
         fail(MAFM_E_DEVICE, "the relax kernel stopped at its watchdog time limit");
 }
@@ -662,9 +665,7 @@ Relax32Config default_config(long long n_cols, int max_terms, const mafm_run_opt
     c.smem_terms = std::min(std::max(max_terms, 1) + 2, 402);
     c.smem_terms = (c.smem_terms + 1) & ~1;
     c.blocks = 0;
-    // Persistent-kernel time limit; MAFM_WATCHDOG_S overrides the 120 s default.
-    const char* w = getenv("MAFM_WATCHDOG_S");
-    c.watchdog_s = w ? atof(w) : 120.0;
+    c.watchdog_ns = watchdog_ns_from_env();
     return c;
 }
 
@@ -924,6 +925,8 @@ int mafm_scan_sample(mafm_scan* scan, int32_t precision, int32_t what, const dou
         if (!scan || (n > 0 && (!pts || !out))) fail(MAFM_E_INVALID, "null argument");
         if (n <= 0) return;
         cuda_check(cudaSetDevice(scan->device), "cudaSetDevice");
+        if (precision != MAFM_FP64 && precision != MAFM_FP32C)
+            fail(MAFM_E_INVALID, "unknown precision %d", precision);
         const bool fp64 = precision == MAFM_FP64;
         ensure_grid(*scan, fp64, nullptr);
         DevBuf<double> dp, dout;
@@ -956,7 +959,8 @@ int mafm_scan_grid_info(const mafm_scan* scan, int32_t what, int32_t n[3], doubl
 int mafm_scan_build_grid(mafm_scan* scan, int32_t precision, void* stream) {
     return guarded([&] {
         if (!scan) fail(MAFM_E_INVALID, "null scan");
-        if (precision != MAFM_FP64 && precision != MAFM_FP32C) fail(MAFM_E_INVALID, "unknown precision %d", precision);
+        if (precision != MAFM_FP64 && precision != MAFM_FP32C)
+            fail(MAFM_E_INVALID, "unknown precision %d", precision);
         if (!scan->d.rigidgrid) return;
         cuda_check(cudaSetDevice(scan->device), "cudaSetDevice");
         ensure_grid(*scan, precision == MAFM_FP64, (cudaStream_t)stream, true);

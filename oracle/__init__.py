@@ -22,11 +22,17 @@ REF_CLI = os.path.join(REF_DIR, "mechafm-omp")
 _port = None
 
 
+def reference_dir(reference: str | None = None) -> str | None:
+    """The reference checkout: the argument, else $MAFM_REFERENCE_DIR, else None."""
+    return reference or os.environ.get("MAFM_REFERENCE_DIR") or None
+
+
 def build(reference: str | None = None) -> None:
-    """Build the port (gcc) and, when the reference sources exist, oracle/_ref."""
+    """Build the port (gcc) and, when the reference sources are given (argument
+    or $MAFM_REFERENCE_DIR) and exist, oracle/_ref."""
     subprocess.run(["make", "-s", "-C", HERE, "port"], check=True)
-    ref = reference or "/root/reference"
-    if os.path.isdir(os.path.join(ref, "src")):
+    ref = reference_dir(reference)
+    if ref and os.path.isdir(os.path.join(ref, "src")):
         subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={ref}", "-j8"], check=True)
 
 

@@ -1,7 +1,8 @@
 """Golden vectors of the frequency-shift post-processing, made by the
 reference's own script.
 
-Run here, where the reference exists:  python tests/golden/make_df_golden.py
+Run where the reference exists:
+    MAFM_REFERENCE_DIR=<reference checkout> python tests/golden/make_df_golden.py
 
 simple-vafm-image.py is a Python 2 script that plots with matplotlib and
 writes only images.  This generator runs the script itself, read from the
@@ -49,7 +50,8 @@ sys.path.insert(0, ROOT)
 import oracle  # noqa: E402
 from mechafm_gb300 import synth  # noqa: E402
 
-SCRIPT = "/root/reference/simple-vafm-image.py"
+# the reference checkout comes from $MAFM_REFERENCE_DIR (read-only)
+SCRIPT = os.path.join(oracle.reference_dir() or "", "simple-vafm-image.py")
 STEPS = [0.1, 0.05, 0.2, 0.25, 0.125, 0.3, 0.07, 0.5 / 3]
 
 

@@ -1,6 +1,7 @@
 """Generate the golden fixtures from the reference's own code.
 
-Run here, where the reference sources exist:  python tests/golden/make_golden.py
+Run where the reference sources exist:
+    MAFM_REFERENCE_DIR=<reference checkout> python tests/golden/make_golden.py
 It builds oracle/_ref (the unmodified reference sources, compiled out of tree
 by oracle/Makefile), writes each case's seeded synthetic input files into
 tests/golden/<case>/ and stores the reference's full-precision results for a

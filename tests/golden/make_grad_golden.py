@@ -1,7 +1,8 @@
 """Golden finite differences of the reference's own relaxation, for the
 gradients of libmafm's adjoint (the reference has no derivatives).
 
-Run here, where the reference exists:  python tests/golden/make_grad_golden.py
+Run where the reference exists:
+    MAFM_REFERENCE_DIR=<reference checkout> python tests/golden/make_grad_golden.py
 
 The case is the 60-atom cluster over 3 x 3 pixels and 4 heights relaxed to
 |F| < 1e-10 (minterm f, ftol 1e-10), so that a difference quotient measures

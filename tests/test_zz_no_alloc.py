@@ -78,3 +78,27 @@ def test_noalloc_rejects_too_many_scans_and_host_outputs():
     code = _abi.lib().mafm_run_batch_noalloc(h1, 1, C.byref(opts), o1, None, None)
     assert code == _abi.MAFM_E_INVALID
     assert b"not device memory" in _abi.lib().mafm_last_error()
+
+
+def test_noalloc_leaves_free_device_memory_unchanged():
+    """After one warm-up call (which may load the kernels' module), repeated
+    calls change the device's free memory (cudaMemGetInfo) by not one byte,
+    and a call without statistics still reports success only after the work
+    is done."""
+    import torch
+    scans = [Scan(Input(golden(n).input).desc(), device=0) for n in CASES]
+    run_batch(scans, lanes=1)   # FP32 rigid grid built by the allocating entry point
+    outs = [torch.zeros(s.desc.n_points * 64, dtype=torch.uint8, device="cuda:0") for s in scans]
+    _noalloc(scans, outs)
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info(0)
+    n = len(scans)
+    handles = (C.c_void_p * n)(*[s.handle for s in scans])
+    optrs = (C.c_void_p * n)(*[o.data_ptr() for o in outs])
+    opts = _abi.RunOpts(_abi.FP32C, 1, 0, 0, 0, 0)
+    for _ in range(3):
+        _noalloc(scans, outs)
+        assert _abi.lib().mafm_run_batch_noalloc(handles, n, C.byref(opts), optrs, None, None) == 0
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info(0)
+    assert free1 == free0, (free0, free1)
