@@ -59,15 +59,32 @@ enum { MAFM_UNITS_KCAL = 0, MAFM_UNITS_KJ = 1, MAFM_UNITS_EV = 2 }; /* simulatio
 /* Arithmetic of a run. */
 enum {
     MAFM_FP64 = 0,   /* plain FP64, the reference's operation order */
-    MAFM_FP32C = 1   /* FP32 pair math, compensated sums, FP64 energy check */
+    MAFM_FP32C = 1,  /* FP32 pair math, compensated sums, double-float tip
+                        positions and energies: the fastest path; FIRE's
+                        discrete decisions can differ from FP64's on near-ties
+                        (about 0.07 % of the points of a 60-atom cluster scan
+                        end more than 1e-3 A from the FP64 result) */
+    MAFM_DF = 2      /* double-float: every pair term, sum, position, velocity
+                        and FIRE quantity as an unevaluated sum of two FP32
+                        numbers (48-bit significand) on the FP32 pipes, so FIRE
+                        takes FP64's decisions; a column in which a decision
+                        still came within the double-float error margin of its
+                        threshold is re-relaxed in FP64 (MAFM_PT_FP64) */
 };
 
 /* Per-point status bits (mafm_point.status). */
 enum {
     MAFM_PT_MAXSTEPS = 1,   /* minimiser returned maxsteps without converging */
     MAFM_PT_NONFINITE = 2,  /* a force or energy was NaN/Inf */
-    MAFM_PT_OUTSIDE = 4     /* rigid grid lookup clamped at the border
+    MAFM_PT_OUTSIDE = 4,    /* rigid grid lookup clamped at the border
                                (reference warns, force_grid.cpp:181-217) */
+    MAFM_PT_NEAR_TIE = 8,   /* MAFM_DF: at this or an earlier height of the
+                               column a FIRE decision (convergence test, sign of
+                               P; minimiser.cpp:15-37, 107-124) lay within the
+                               double-float error margin of its threshold */
+    MAFM_PT_FP64 = 16       /* MAFM_DF: the column was then re-relaxed in FP64
+                               from its first height: the point holds the plain
+                               FP64 kernel's bits */
 };
 
 /* One tip–atom van der Waals pair.  LJ: p = {es6, es12, 0} with
@@ -161,7 +178,7 @@ typedef struct mafm_run_stats {
     uint64_t force_evals;       /* tip force evaluations, output evaluations included */
     uint64_t pair_evals;        /* tip–atom pair terms evaluated (vdW + Coulomb) */
     uint32_t error_word;        /* OR of MAFM_PT_* over all points, plus device error bits */
-    uint32_t reserved;
+    uint32_t fp64_columns;      /* MAFM_DF: columns re-relaxed in FP64 */
     double kernel_ms;           /* device time of the relax kernel(s) */
 } mafm_run_stats;
 
@@ -257,9 +274,20 @@ int mafm_scan_size(const mafm_scan* scan, int64_t* n_points, int64_t* n_columns)
 int mafm_run(mafm_scan* scan, const mafm_run_opts* opts, mafm_point* out,
              mafm_run_stats* stats, void* stream);
 
-/* Relax several scans in one persistent launch (MAFM_FP32C only).  outs[s]
- * receives scan s's points; all outs must be device memory, or all host
- * (pinned host outputs are written directly, as for mafm_run). */
+/* Relax chosen pixel columns of a scan in plain FP64: for pixels (i, j)
+ * given as columns[m] = i*ny + j, in any order and from anywhere in the scan,
+ * out[m*nz + k] receives height k (n*nz records, host or device memory, as
+ * for mafm_run).  One warp relaxes one column and adds every sum in the
+ * reference's order, so the points are bit-identical to mafm_run's MAFM_FP64
+ * points.  The pixel loop of Simulation::run (simulation.cpp:78-122) over a
+ * sample of pixels: used to check a fast run against FP64 on pixels spread
+ * over the whole scan.  Synchronises the stream. */
+int mafm_run_columns(mafm_scan* scan, const int32_t* columns, int64_t n, mafm_point* out,
+                     mafm_run_stats* stats, void* stream);
+
+/* Relax several scans in one persistent launch (MAFM_FP32C or MAFM_DF).
+ * outs[s] receives scan s's points; all outs must be device memory, or all
+ * host (pinned host outputs are written directly, as for mafm_run). */
 int mafm_run_batch(mafm_scan* const* scans, int32_t n_scans, const mafm_run_opts* opts,
                    mafm_point* const* outs, mafm_run_stats* stats, void* stream);
 

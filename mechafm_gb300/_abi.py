@@ -22,8 +22,8 @@ MIN_SD, MIN_FIRE = 0, 1
 INT_EULER, INT_MIDPOINT, INT_RK4 = 0, 1, 2
 TERM_E, TERM_F, TERM_EF = 0, 1, 2
 PAIR_LJ, PAIR_MORSE = 0, 1
-FP64, FP32C = 0, 1
-PT_MAXSTEPS, PT_NONFINITE, PT_OUTSIDE = 1, 2, 4
+FP64, FP32C, DF = 0, 1, 2
+PT_MAXSTEPS, PT_NONFINITE, PT_OUTSIDE, PT_NEAR_TIE, PT_FP64 = 1, 2, 4, 8, 16
 NOALLOC_MAX_SCANS = 32
 
 
@@ -74,7 +74,7 @@ class RunOpts(C.Structure):
 class RunStats(C.Structure):
     _fields_ = [("total_steps", C.c_uint64), ("force_evals", C.c_uint64),
                 ("pair_evals", C.c_uint64), ("error_word", C.c_uint32),
-                ("reserved", C.c_uint32), ("kernel_ms", C.c_double)]
+                ("fp64_columns", C.c_uint32), ("kernel_ms", C.c_double)]
 
 
 class FlexDesc(C.Structure):
@@ -115,6 +115,7 @@ SIGNATURES = {
     "mafm_scan_destroy": (C.c_int, [_P]),
     "mafm_scan_size": (C.c_int, [_P, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
     "mafm_run": (C.c_int, [_P, C.POINTER(RunOpts), _P, C.POINTER(RunStats), _P]),
+    "mafm_run_columns": (C.c_int, [_P, _P, C.c_int64, _P, C.POINTER(RunStats), _P]),
     "mafm_run_batch": (C.c_int, [C.POINTER(_P), C.c_int32, C.POINTER(RunOpts),
                                  C.POINTER(_P), C.POINTER(RunStats), _P]),
     "mafm_run_batch_noalloc": (C.c_int, [C.POINTER(_P), C.c_int32, C.POINTER(RunOpts),

@@ -51,6 +51,7 @@ def _units():
     return [
         ([nv] + common + ["-fmad=false", os.path.join(CSRC, "relax64.cu")], "relax64.o"),
         ([nv] + common + [os.path.join(CSRC, "relax32.cu")], "relax32.o"),
+        ([nv] + common + [os.path.join(CSRC, "relaxdf.cu")], "relaxdf.o"),
         ([nv] + common + [os.path.join(CSRC, "scan.cu")], "scan.o"),
         ([nv] + common + [os.path.join(CSRC, "noalloc.cu")], "noalloc.o"),
         ([nv] + common + [os.path.join(CSRC, "adjoint.cu")], "adjoint.o"),

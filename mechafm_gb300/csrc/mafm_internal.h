@@ -155,7 +155,9 @@ struct RunCounters {
     unsigned long long force_evals;
     unsigned long long pair_evals;
     unsigned int error_word;
-    unsigned int pad;
+    unsigned int n_tie;               // MAFM_DF: columns listed for FP64 re-relaxation
+                                      // (may exceed the list's capacity)
+    unsigned long long repair_next;   // queue head of the re-relaxation kernel
 };
 
 // Launchers implemented in relax64.cu / relax32.cu.  ctr points to zeroed
@@ -190,6 +192,15 @@ struct Relax32Config {
 
 cudaError_t launch_relax32(const BatchScan* scans_dev, int n_scans, long long n_tiles,
                            const Relax32Config& cfg, RunCounters* ctr, cudaStream_t s);
+// FP64 re-relaxation of listed columns (relax64.cu): list[i] = scan index << 32
+// | column for i < min(count, cap), where count = ctr->n_tie when n_fixed < 0
+// (the columns the double-float kernel flagged) and n_fixed otherwise.
+// replace = true marks the points MAFM_PT_FP64 and corrects the step total
+// for the records it overwrites.  The points of column c go to
+// out + (c - col_begin) nz, or with list_out to out + i nz for list entry i.
+cudaError_t launch_repair64(const BatchScan* scans, const unsigned long long* list, unsigned cap,
+                            long long n_fixed, bool replace, bool list_out, RunCounters* ctr,
+                            cudaStream_t s);
 cudaError_t launch_sample32(const ScanParams& p, int what, const double* pts, int64_t n,
                             double* out, RunCounters* ctr, cudaStream_t s);
 cudaError_t launch_grid_build32(const ScanParams& p, const GridView& g, float4* out,

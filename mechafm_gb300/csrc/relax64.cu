@@ -16,15 +16,12 @@
 //   pixel column, z descent    simulation.cpp:93-122, system.cpp:28-51, 139-162
 //   rigid grid build           simulation.cpp:420-501
 #include "mafm_internal.h"
+#include "relax_tpl.cuh"
 
 namespace mafm {
 namespace {
 
-struct V3 {
-    double x, y, z;
-};
-
-__device__ __forceinline__ double len3(V3 v) { return sqrt(v.x * v.x + v.y * v.y + v.z * v.z); }
+using V3 = V3T<double>;
 
 // LJInteraction::eval / MorseInteraction::eval; r = tip - (atom + shift).
 __device__ __forceinline__ void vdw64(int kind, double p0, double p1, double p2, V3 r, V3& f,
@@ -115,6 +112,33 @@ __device__ void interp64(const GridView& g, V3 pos, V3& f, double& e, int& outsi
     f.x = out[0]; f.y = out[1]; f.z = out[2]; e = out[3];
 }
 
+// The tip–dummy van der Waals (+ Coulomb) term and the XY spring, added to
+// the tip–surface force and energy in Eval64::all's order
+// (simulation.cpp:503-515, interactions.cpp:252-266).
+__device__ __forceinline__ void add_tip_dummy(const ScanParams& p, V3 tip, V3 dum, V3& F,
+                                              double& E) {
+    V3 f;
+    double e;
+    V3 r = {dum.x - tip.x, dum.y - tip.y, dum.z - tip.z};
+    vdw64(p.td_kind, p.td_p[0], p.td_p[1], p.td_p[2], r, f, e);
+    F.x -= f.x; F.y -= f.y; F.z -= f.z; E += e;
+    if (p.td_coul) {
+        coul64(p.td_qq, r, f, e);
+        F.x -= f.x; F.y -= f.y; F.z -= f.z; E += e;
+    }
+    double rx = dum.x - tip.x, ry = dum.y - tip.y;
+    double rr = sqrt(rx * rx + ry * ry);
+    double dr = rr - p.harm_r0;
+    double eh = p.harm_k * dr * dr;
+    double fx = 0, fy = 0;
+    if (rr > 1e-10) {
+        double s = -2 * p.harm_k * dr / rr;
+        fx = s * rx; fy = s * ry;
+    }
+    F.x -= fx; F.y -= fy; F.z -= 0.0;
+    E += eh;
+}
+
 struct Eval64 {
     const ScanParams& p;
     const AtomRec64* atoms;   // shared or global copy of the terms
@@ -156,157 +180,97 @@ struct Eval64 {
     // All interactions of the relaxation (integrators.cpp evaluate them all).
     __device__ void all(V3 tip, V3 dum, V3& F, double& E, int& outside) {
         ts(tip, F, E, outside);
-        V3 f;
-        double e;
-        V3 r = {dum.x - tip.x, dum.y - tip.y, dum.z - tip.z};
-        vdw64(p.td_kind, p.td_p[0], p.td_p[1], p.td_p[2], r, f, e);
-        F.x -= f.x; F.y -= f.y; F.z -= f.z; E += e;
-        if (p.td_coul) {
-            coul64(p.td_qq, r, f, e);
-            F.x -= f.x; F.y -= f.y; F.z -= f.z; E += e;
-        }
-        double rx = dum.x - tip.x, ry = dum.y - tip.y;
-        double rr = sqrt(rx * rx + ry * ry);
-        double dr = rr - p.harm_r0;
-        double eh = p.harm_k * dr * dr;
-        double fx = 0, fy = 0;
-        if (rr > 1e-10) {
-            double s = -2 * p.harm_k * dr / rr;
-            fx = s * rx; fy = s * ry;
-        }
-        F.x -= fx; F.y -= fy; F.z -= 0.0;
-        E += eh;
+        add_tip_dummy(p, tip, dum, F, E);
     }
+
+    // The FP64 path makes the reference's decisions itself: nothing to watch.
+    __device__ void watch_conv(const ScanParams&, V3, double) {}
+    __device__ void watch_p(double, double, double) {}
+    __device__ int column_status() const { return 0; }
 };
 
-__device__ __forceinline__ bool converged64(const ScanParams& p, V3 F, double ediff) {
-    if (p.minterm == MAFM_TERM_E) return fabs(ediff) < p.etol;
-    if (p.minterm == MAFM_TERM_F) return len3(F) < p.ftol;
-    return fabs(ediff) < p.etol && len3(F) < p.ftol;
-}
+// Terms per chunk of the warp-cooperative evaluation (two per lane).
+constexpr int kWarpChunk = 64;
 
-struct State64 {
-    V3 tip, vel, dum;
-    double energy;
-    int outside;
-};
+// The same sums as Eval64, evaluated by a whole warp for one column: lane l
+// computes terms l, l + 32, ... of a chunk into the warp's shared buffer, then
+// lanes 0-3 add component x, y, z, E of every term in the reference's order
+// (vdW part, then Coulomb part, term by term), so each sum is formed by the
+// same sequence of FP64 additions as in Eval64 and the results are
+// bit-identical.  A term without Coulomb contributes an exact +0, which
+// leaves a sum that starts at +0 unchanged.  Every lane ends with the sums,
+// and every lane runs the (warp-uniform) minimiser on them.
+struct EvalWarp64 {
+    const ScanParams& p;
+    const AtomRec64* atoms;
+    int n;
+    int mode;                 // ts_mode
+    int lane;
+    Node64* buf;              // 2 * kWarpChunk records {x, y, z, E} of this warp
+    unsigned err;
+    unsigned long long pairs; // counted on lane 0
 
-// FIREMinimisation, minimiser.cpp:67-129 (only the tip is free).
-__device__ int fire64(Eval64& ev, const ScanParams& p, State64& s, unsigned long long& evals) {
-    const int n_min = 5;
-    const double f_inc = 1.1, f_dec = 0.5, f_a = 0.99, a_start = 0.1;
-    const double dt_max = 10 * p.dt;
-    double alpha = a_start, dt = p.dt;
-    int n_non_neg = 0;
-    int n_tot = 1;
-    for (; n_tot < p.maxsteps; ++n_tot) {
-        const double prev = s.energy;
-        V3 F, pp = s.tip, v = s.vel;
-        double E;
-        if (p.integrator == MAFM_INT_EULER) {
-            ev.all(pp, s.dum, F, E, s.outside);
-            evals += 1;
-            s.tip.x = pp.x + dt * v.x; s.tip.y = pp.y + dt * v.y; s.tip.z = pp.z + dt * v.z;
-            s.vel.x = v.x + dt * F.x / 1.0; s.vel.y = v.y + dt * F.y / 1.0; s.vel.z = v.z + dt * F.z / 1.0;
-        } else if (p.integrator == MAFM_INT_MIDPOINT) {
-            V3 f1, f2;
-            double e1, e2;
-            ev.all(pp, s.dum, f1, e1, s.outside);
-            V3 p2 = {pp.x + dt / 2 * v.x, pp.y + dt / 2 * v.y, pp.z + dt / 2 * v.z};
-            V3 v2 = {v.x + dt / 2 * f1.x / 1.0, v.y + dt / 2 * f1.y / 1.0, v.z + dt / 2 * f1.z / 1.0};
-            ev.all(p2, s.dum, f2, e2, s.outside);
-            evals += 2;
-            s.tip.x = pp.x + dt * v2.x; s.tip.y = pp.y + dt * v2.y; s.tip.z = pp.z + dt * v2.z;
-            s.vel.x = v.x + dt * f2.x / 1.0; s.vel.y = v.y + dt * f2.y / 1.0; s.vel.z = v.z + dt * f2.z / 1.0;
-            F = f2;
-            E = e2;
-        } else {
-            V3 f1, f2, f3, f4;
-            double e1, e2, e3, e4;
-            ev.all(pp, s.dum, f1, e1, s.outside);
-            V3 p2 = {pp.x + dt / 2 * v.x, pp.y + dt / 2 * v.y, pp.z + dt / 2 * v.z};
-            V3 v2 = {v.x + dt / 2 * f1.x / 1.0, v.y + dt / 2 * f1.y / 1.0, v.z + dt / 2 * f1.z / 1.0};
-            ev.all(p2, s.dum, f2, e2, s.outside);
-            V3 p3 = {pp.x + dt / 2 * v2.x, pp.y + dt / 2 * v2.y, pp.z + dt / 2 * v2.z};
-            V3 v3 = {v.x + dt / 2 * f2.x / 1.0, v.y + dt / 2 * f2.y / 1.0, v.z + dt / 2 * f2.z / 1.0};
-            ev.all(p3, s.dum, f3, e3, s.outside);
-            V3 p4 = {pp.x + dt * v3.x, pp.y + dt * v3.y, pp.z + dt * v3.z};
-            V3 v4 = {v.x + dt * f3.x / 1.0, v.y + dt * f3.y / 1.0, v.z + dt * f3.z / 1.0};
-            ev.all(p4, s.dum, f4, e4, s.outside);
-            evals += 4;
-            s.tip.x = pp.x + dt / 6 * (v.x + 2 * v2.x + 2 * v3.x + v4.x);
-            s.tip.y = pp.y + dt / 6 * (v.y + 2 * v2.y + 2 * v3.y + v4.y);
-            s.tip.z = pp.z + dt / 6 * (v.z + 2 * v2.z + 2 * v3.z + v4.z);
-            s.vel.x = v.x + dt / 6 * (f1.x + 2 * f2.x + 2 * f3.x + f4.x) / 1.0;
-            s.vel.y = v.y + dt / 6 * (f1.y + 2 * f2.y + 2 * f3.y + f4.y) / 1.0;
-            s.vel.z = v.z + dt / 6 * (f1.z + 2 * f2.z + 2 * f3.z + f4.z) / 1.0;
-            F.x = (f1.x + 2 * f2.x + 2 * f3.x + f4.x) / 6;
-            F.y = (f1.y + 2 * f2.y + 2 * f3.y + f4.y) / 6;
-            F.z = (f1.z + 2 * f2.z + 2 * f3.z + f4.z) / 6;
-            E = (e1 + 2 * e2 + 2 * e3 + e4) / 6;
+    __device__ void ts(V3 tip, V3& F, double& E, int& outside) {
+        if (mode == 2) {
+            // the rigid grid: one lookup, the same on every lane (Eval64::ts)
+            V3 f;
+            double e;
+            interp64(p.grid, tip, f, e, outside, err);
+            F.x = 0.0 + f.x; F.y = 0.0 + f.y; F.z = 0.0 + f.z;
+            E = 0.0 + e;
+            return;
         }
-        s.energy = E;
-        if (converged64(p, F, E - prev)) break;
-        const V3 w = s.vel;
-        const double pw = w.x * F.x + w.y * F.y + w.z * F.z;
-        const double fl = len3(F);
-        V3 fh = {0, 0, 0};
-        if (fl > 1e-10) { fh.x = F.x / fl; fh.y = F.y / fl; fh.z = F.z / fl; }
-        const double vl = len3(w);
-        s.vel.x = (1 - alpha) * w.x + alpha * fh.x * vl;
-        s.vel.y = (1 - alpha) * w.y + alpha * fh.y * vl;
-        s.vel.z = (1 - alpha) * w.z + alpha * fh.z * vl;
-        if (pw < 0) {
-            s.vel.x = s.vel.y = s.vel.z = 0;
-            n_non_neg = 0;
-            dt *= f_dec;
-            alpha = a_start;
-        } else {
-            if (n_non_neg > n_min) {
-                const double g = dt * f_inc;
-                dt = dt_max < g ? dt_max : g;   // std::min(g, dt_max)
-                alpha *= f_a;
+        double acc = 0.0;   // lane m < 4: component m of {Fx, Fy, Fz, E}
+        for (int base = 0; base < n; base += kWarpChunk) {
+            const int cnt = min(kWarpChunk, n - base);
+            for (int j = lane; j < cnt; j += 32) {
+                const AtomRec64 t = atoms[base + j];
+                V3 r = {tip.x - t.x, tip.y - t.y, tip.z - t.z};
+                V3 f;
+                double e;
+                vdw64(t.kind, t.p0, t.p1, t.p2, r, f, e);
+                buf[2 * j] = Node64{f.x, f.y, f.z, e};
+                if (t.coul) {
+                    coul64(t.qq, r, f, e);
+                    buf[2 * j + 1] = Node64{f.x, f.y, f.z, e};
+                } else {
+                    buf[2 * j + 1] = Node64{0.0, 0.0, 0.0, 0.0};
+                }
             }
-            n_non_neg++;
+            __syncwarp();
+            if (lane < 4) {
+                const double* b = reinterpret_cast<const double*>(buf) + lane;
+                for (int j = 0; j < 2 * cnt; ++j) acc += b[4 * j];
+            }
+            __syncwarp();
         }
+        if (lane == 0) {
+            unsigned long long c = 0;
+            for (int i = 0; i < n; ++i) c += atoms[i].coul ? 1ull : 0ull;
+            pairs += (unsigned long long)n + c;
+        }
+        if (mode == 1) {
+            V3 f;
+            double e;
+            int unused = 0;
+            interp64(p.es, tip, f, e, unused, err);
+            if (lane < 4) acc += lane == 0 ? f.x : lane == 1 ? f.y : lane == 2 ? f.z : e;
+        }
+        F.x = __shfl_sync(0xffffffffu, acc, 0);
+        F.y = __shfl_sync(0xffffffffu, acc, 1);
+        F.z = __shfl_sync(0xffffffffu, acc, 2);
+        E = __shfl_sync(0xffffffffu, acc, 3);
     }
-    return n_tot;
-}
 
-// SDMinimisation, minimiser.cpp:39-65.
-__device__ int sd64(Eval64& ev, const ScanParams& p, State64& s, unsigned long long& evals) {
-    int n = 1;
-    for (; n < p.maxsteps; ++n) {
-        const double prev = s.energy;
-        V3 F;
-        double E;
-        ev.all(s.tip, s.dum, F, E, s.outside);
-        evals += 1;
-        s.energy = E;
-        if (converged64(p, F, E - prev)) break;
-        s.tip.x += p.dt * F.x; s.tip.y += p.dt * F.y; s.tip.z += p.dt * F.z;
+    __device__ void all(V3 tip, V3 dum, V3& F, double& E, int& outside) {
+        ts(tip, F, E, outside);
+        add_tip_dummy(p, tip, dum, F, E);
     }
-    return n;
-}
 
-// System::setDummyXY (system.cpp:139-162)
-__device__ __forceinline__ void dummy_xy64(const ScanParams& p, bool wrap, double x, double y,
-                                           double& ox, double& oy) {
-    if (wrap) {
-        const double* ci = p.cell_inv;
-        const double* c = p.cell;
-        V3 t = {x - p.offset[0], y - p.offset[1], 0 - p.offset[2]};
-        V3 cn = {ci[0] * t.x + ci[1] * t.y + ci[2] * t.z, ci[3] * t.x + ci[4] * t.y + ci[5] * t.z,
-                 ci[6] * t.x + ci[7] * t.y + ci[8] * t.z};
-        cn.x -= floor(cn.x);
-        cn.y -= floor(cn.y);
-        ox = (c[0] * cn.x + c[1] * cn.y + c[2] * cn.z) + p.offset[0];
-        oy = (c[3] * cn.x + c[4] * cn.y + c[5] * cn.z) + p.offset[1];
-    } else {
-        ox = x;
-        oy = y;
-    }
-}
+    __device__ void watch_conv(const ScanParams&, V3, double) {}
+    __device__ void watch_p(double, double, double) {}
+    __device__ int column_status() const { return 0; }
+};
 
 // Stage the terms into shared memory when they fit.
 __device__ const AtomRec64* stage64(const ScanParams& p, AtomRec64* sm, int cap) {
@@ -324,47 +288,65 @@ __global__ void __launch_bounds__(128) relax64_kernel(const ScanParams p, mafm_p
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const AtomRec64* atoms = stage64(p, reinterpret_cast<AtomRec64*>(smem_raw), smem_cap);
     Eval64 ev{p, atoms, p.n_terms_direct, p.ts_mode, 0u, 0ull};
-    unsigned long long steps = 0, evals = 0;
+    long long steps = 0;
+    unsigned long long evals = 0;
     unsigned status_or = 0;
-    const bool wrap = p.tip_pbc && p.ts_mode != 2;
     for (;;) {
         const long long c = (long long)atomicAdd(&ctr->next_work, 1ull) + col_begin;
         if (c >= col_end) break;
-        const int i = (int)(c / p.ny), j = (int)(c % p.ny);
-        State64 s;
-        s.vel = {0, 0, 0};
-        s.energy = 0;
-        double x, y;
-        dummy_xy64(p, wrap, i * p.dx, j * p.dy, x, y);
-        s.dum = {x, y, p.zhigh};
-        s.tip = {x, y, p.zhigh - p.tip_dummy_d};
-        mafm_point* o = out + (size_t)(c - col_begin) * p.nz;
-        for (int k = 0; k < p.nz; ++k) {
-            s.outside = 0;
-            const int n = p.minimiser == MAFM_MIN_SD ? sd64(ev, p, s, evals) : fire64(ev, p, s, evals);
-            V3 F;
-            double E;
-            ev.ts(s.tip, F, E, s.outside);
-            evals += 1;
-            int st = (n >= p.maxsteps ? MAFM_PT_MAXSTEPS : 0) | (s.outside ? MAFM_PT_OUTSIDE : 0);
-            if (!isfinite(F.x) || !isfinite(F.y) || !isfinite(F.z) || !isfinite(E)) st |= MAFM_PT_NONFINITE;
-            mafm_point r;
-            r.tip[0] = s.tip.x; r.tip[1] = s.tip.y; r.tip[2] = s.tip.z;
-            r.force[0] = F.x; r.force[1] = F.y; r.force[2] = F.z;
-            r.energy = E;
-            r.steps = n;
-            r.status = st;
-            o[k] = r;
-            status_or |= (unsigned)st;
-            steps += (unsigned long long)n;
-            s.dum.z -= p.dz;
-            s.tip.z -= p.dz;
-        }
+        relax_column_t<double>(ev, p, c, out + (size_t)(c - col_begin) * p.nz, true, false, steps, evals,
+                       status_or);
     }
-    atomicAdd(&ctr->total_steps, steps);
+    atomicAdd(&ctr->total_steps, (unsigned long long)steps);
     atomicAdd(&ctr->force_evals, evals);
     atomicAdd(&ctr->pair_evals, ev.pairs);
     if (status_or | ev.err) atomicOr(&ctr->error_word, status_or | ev.err);
+}
+
+// FP64 relaxation of listed columns (scan << 32 | column), one warp per
+// column: the re-relaxation of the double-float kernel's near-tie columns
+// (replace = true), or a plain FP64 run of chosen columns.  Persistent: each
+// warp takes the next listed column and relaxes it from its top height with
+// EvalWarp64, which forms every sum exactly as relax64_kernel does, so the
+// column holds the plain FP64 kernel's bits.  A replacement corrects the step
+// total by the difference; force and pair evaluations count every pass.
+__global__ void __launch_bounds__(128) repair64_kernel(const BatchScan* __restrict__ scans,
+                                                       const unsigned long long* __restrict__ list,
+                                                       unsigned cap, long long n_fixed,
+                                                       bool replace, bool list_out,
+                                                       RunCounters* ctr) {
+    extern __shared__ __align__(32) unsigned char rraw[];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    Node64* buf = reinterpret_cast<Node64*>(rraw) + (size_t)warp * 2 * kWarpChunk;
+    const unsigned long long count =
+        n_fixed >= 0 ? (unsigned long long)n_fixed : (unsigned long long)ctr->n_tie;
+    const unsigned long long listed = min(count, (unsigned long long)cap);
+    long long steps = 0;
+    unsigned long long evals = 0, pairs = 0;
+    unsigned status_or = 0, err = 0;
+    for (;;) {
+        unsigned long long t = 0;
+        if (lane == 0) t = atomicAdd(&ctr->repair_next, 1ull);
+        t = __shfl_sync(0xffffffffu, t, 0);
+        if (t >= listed) break;
+        const unsigned long long e = list[t];
+        const BatchScan& B = scans[(int)(e >> 32)];
+        const long long c = (long long)(unsigned)(e & 0xffffffffull);
+        const ScanParams& p = B.p;
+        EvalWarp64 ev{p, p.atoms64, p.n_terms_direct, p.ts_mode, lane, buf, 0u, 0ull};
+        mafm_point* o = B.out + (size_t)(list_out ? (long long)t : c - B.col_begin) * p.nz;
+        relax_column_t<double>(ev, p, c, o, lane == 0, replace, steps,
+                       evals, status_or);
+        pairs += ev.pairs;
+        err |= ev.err;
+        __syncwarp();
+    }
+    if (lane == 0) {
+        atomicAdd(&ctr->total_steps, (unsigned long long)steps);
+        atomicAdd(&ctr->force_evals, evals);
+        atomicAdd(&ctr->pair_evals, pairs);
+        if (status_or | err) atomicOr(&ctr->error_word, status_or | err);
+    }
 }
 
 __global__ void sample64_kernel(const ScanParams p, int what, const double* pts, long long n,
@@ -400,7 +382,8 @@ __global__ void __launch_bounds__(128) grid_build64_kernel(const ScanParams p, c
         const long long ij = idx / g.n[2];
         const int j = (int)(ij % g.n[1]), i = (int)(ij / g.n[1]);
         double x, y;
-        dummy_xy64(p, p.tip_pbc != 0, i * g.basis[0] + g.origin[0], j * g.basis[4] + g.origin[1], x, y);
+        dummy_xy_t<double>(p, p.tip_pbc != 0, i * g.basis[0] + g.origin[0],
+                           j * g.basis[4] + g.origin[1], x, y);
         V3 tip = {x, y, k * g.basis[8] + g.origin[2]};
         V3 F;
         double E;
@@ -438,6 +421,20 @@ cudaError_t launch_relax64(const ScanParams& p, mafm_point* out, RunCounters* ct
     if (blocks > need) blocks = need;
     if (blocks < 1) blocks = 1;
     relax64_kernel<<<(unsigned)blocks, 128, sm, s>>>(p, out, ctr, col_begin, col_end, cap);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_repair64(const BatchScan* scans, const unsigned long long* list, unsigned cap,
+                            long long n_fixed, bool replace, bool list_out, RunCounters* ctr,
+                            cudaStream_t s) {
+    constexpr int kThreads = 128;
+    const size_t smem = (size_t)(kThreads / 32) * 2 * kWarpChunk * sizeof(Node64);
+    unsigned blocks = (unsigned)sm_count();
+    if (n_fixed >= 0) {
+        const long long need = (std::min<long long>(n_fixed, cap) + kThreads / 32 - 1) / (kThreads / 32);
+        blocks = (unsigned)std::max(1ll, std::min<long long>(need, 8ll * sm_count()));
+    }
+    repair64_kernel<<<blocks, kThreads, smem, s>>>(scans, list, cap, n_fixed, replace, list_out, ctr);
     return cudaGetLastError();
 }
 

@@ -20,6 +20,7 @@
 #include <cstring>
 #include <vector>
 
+#include "mafm_df.h"
 #include "mafm_internal.h"
 
 namespace mafm {
@@ -175,6 +176,7 @@ __global__ void nodes_to_float4(const Node64* in, float4* out, long long n) {
 }
 
 __global__ void write_batch(BatchScan* dst, BatchScan v) { *dst = v; }
+__global__ void write_batch_df(BatchDF* dst, BatchDF v) { *dst = v; }
 
 // Expected relaxation cost of each pixel column: the density of tip–atom terms
 // under the pixel (Gaussian of 2 A in xy).  Columns over the molecule take up
@@ -218,6 +220,10 @@ struct mafm_scan {
     mafm::DevBuf<mafm::BatchScan> batch;
     mafm::DevBuf<mafm_point> stage;
     mafm::DevBuf<int> order;             // columns by descending expected cost
+    mafm::DevBuf<mafm::AtomRecDF> atomsdf;     // terms in double-float (MAFM_DF)
+    mafm::DevBuf<mafm::NodeDF> esdf;           // external field in double-float
+    mafm::DevBuf<mafm::BatchDF> batchdf;       // descriptor of a double-float run
+    mafm::DevBuf<unsigned long long> repair;   // columns to re-relax in FP64
     bool order_built = false;
     mafm::RunCounters* host_ctr = nullptr;   // pinned
     int n_pairs_per_eval = 0;
@@ -373,6 +379,14 @@ void pack_terms(mafm_scan& s, const mafm_scan_desc& d) {
         cuda_check(cudaMemcpy(s.atoms32.p, t32.data(), t32.size() * sizeof(AtomRec32),
                               cudaMemcpyHostToDevice), "upload terms");
     }
+    // double-float copy for MAFM_DF
+    std::vector<AtomRecDF> tdf;
+    tdf.reserve(t64.size());
+    for (const AtomRec64& r : t64) tdf.push_back(term_df(r));
+    s.atomsdf.alloc(std::max<size_t>(tdf.size(), 1));
+    if (!tdf.empty())
+        cuda_check(cudaMemcpy(s.atomsdf.p, tdf.data(), tdf.size() * sizeof(AtomRecDF),
+                              cudaMemcpyHostToDevice), "upload terms");
     s.P.n_terms = (int)t64.size();
     s.P.n_terms_direct = d.rigidgrid ? 0 : s.P.n_terms;
     s.has_coulomb = n_coul > 0;
@@ -470,6 +484,8 @@ void build_external_field(mafm_scan& s, const mafm_scan_desc& d) {
     }
     s.es32.alloc((size_t)N);
     nodes_to_float4<<<nb, 256>>>(s.es64.p, s.es32.p, N);
+    s.esdf.alloc((size_t)N);
+    cuda_check(launch_nodes_to_df(s.es64.p, s.esdf.p, N, nullptr), "external field (double-float)");
     cuda_check(cudaDeviceSynchronize(), "external field");
     unsigned long long bits = 0;
     cuda_check(cudaMemcpy(&bits, maxbits.p, sizeof bits, cudaMemcpyDeviceToHost), "readback");
@@ -629,6 +645,30 @@ void check_device_errors(const RunCounters& c) {
         fail(MAFM_E_DEVICE, "the relax kernel stopped at its watchdog time limit");
 }
 
+// The double-float path relaxes pair terms and the external field; a rigid
+// grid would need a double-float grid build.
+void check_df_supported(const mafm_scan& s) {
+    if (s.d.rigidgrid)
+        fail(MAFM_E_UNSUPPORTED, "MAFM_DF relaxes over pair terms and the external field; a scan "
+                                 "with a rigid force grid runs in MAFM_FP64 or MAFM_FP32C");
+}
+
+// Descriptor of a double-float run over columns [cb, ce) of a scan.
+BatchDF batch_df_entry(const mafm_scan& s, mafm_point* out, int cb, int ce, bool whole,
+                       long long col_first) {
+    BatchDF b{};
+    ScanParams p = s.P;
+    p.n_terms_direct = p.n_terms;
+    b.p = params_df(p, s.atomsdf.p, s.esdf.p);
+    b.out = out;
+    b.col_first = col_first;
+    b.col_begin = cb;
+    b.col_end = ce;
+    b.order = whole && s.order_built ? s.order.p : nullptr;
+    b.n_pairs_per_eval = s.n_pairs_per_eval;
+    return b;
+}
+
 // Default FP32 launch shape (the autotuner's measurements behind it: 401 x 401
 // cluster, 101 x 101 graphene, 128 x 128 cluster, 256-scan batch).
 // Lanes per column: the fewest that give a quarter of the resident lanes a
@@ -767,7 +807,9 @@ int mafm_run(mafm_scan* scan, const mafm_run_opts* opts, mafm_point* out, mafm_r
                 fail(MAFM_E_INVALID, "column range [%d, %d) outside [0, %lld)", cb, ce, n_cols_all);
         }
         const int prec = opts ? opts->precision : MAFM_FP64;
-        if (prec != MAFM_FP64 && prec != MAFM_FP32C) fail(MAFM_E_INVALID, "precision %d", prec);
+        if (prec != MAFM_FP64 && prec != MAFM_FP32C && prec != MAFM_DF)
+            fail(MAFM_E_INVALID, "precision %d", prec);
+        if (prec == MAFM_DF) check_df_supported(*scan);
         const size_t n_pts = (size_t)(ce - cb) * scan->d.nz;
         if (n_pts == 0) {
             if (stats) *stats = mafm_run_stats{};
@@ -784,11 +826,32 @@ int mafm_run(mafm_scan* scan, const mafm_run_opts* opts, mafm_point* out, mafm_r
             dout = scan->stage.p;
         }
         ensure_grid(*scan, prec == MAFM_FP64, st);
+        const bool whole = cb == 0 && ce == n_cols_all;
+        if (prec == MAFM_DF && whole) ensure_order(*scan, st);
         zero_counters(*scan, st);
         cuda_check(cudaEventRecord(scan->ev0, st), "cudaEventRecord");
         if (prec == MAFM_FP64) {
             ScanParams p = build_params(*scan);
             cuda_check(launch_relax64(p, dout, scan->ctr.p, cb, ce, st), "relax64 launch");
+        } else if (prec == MAFM_DF) {
+            // double-float relaxation, then FP64 for the columns it lists
+            BatchScan b{};
+            b.p = build_params(*scan);
+            b.out = dout;
+            b.col_begin = cb;
+            b.col_end = ce;
+            b.n_pairs_per_eval = scan->n_pairs_per_eval;
+            b.has_coulomb = scan->has_coulomb;
+            write_batch<<<1, 1, 0, st>>>(scan->batch.p, b);
+            scan->batchdf.alloc(1);
+            write_batch_df<<<1, 1, 0, st>>>(scan->batchdf.p, batch_df_entry(*scan, dout, cb, ce, whole, 0));
+            cuda_check(cudaGetLastError(), "descriptor upload");
+            const unsigned cap = (unsigned)(ce - cb);
+            scan->repair.alloc(cap);
+            cuda_check(launch_relaxdf(scan->batchdf.p, 1, ce - cb, scan->ctr.p, scan->repair.p, cap,
+                                      watchdog_ns_from_env(), st), "double-float relax launch");
+            cuda_check(launch_repair64(scan->batch.p, scan->repair.p, cap, -1, true, false, scan->ctr.p, st),
+                       "FP64 re-relaxation launch");
         } else {
             BatchScan b{};
             b.p = build_params(*scan);
@@ -823,7 +886,7 @@ int mafm_run(mafm_scan* scan, const mafm_run_opts* opts, mafm_point* out, mafm_r
                 stats->force_evals = c.force_evals;
                 stats->pair_evals = c.pair_evals;
                 stats->error_word = c.error_word;
-                stats->reserved = 0;
+                stats->fp64_columns = prec == MAFM_DF ? std::min<unsigned>(c.n_tie, ce - cb) : 0;
                 stats->kernel_ms = ms;
             }
             check_device_errors(c);
@@ -835,10 +898,12 @@ int mafm_run_batch(mafm_scan* const* scans, int32_t n_scans, const mafm_run_opts
                    mafm_point* const* outs, mafm_run_stats* stats, void* stream) {
     return guarded([&] {
         if (!scans || !outs || n_scans <= 0) fail(MAFM_E_INVALID, "empty batch");
-        if (opts && opts->precision != MAFM_FP32C)
-            fail(MAFM_E_UNSUPPORTED, "batched runs use MAFM_FP32C");
+        const int prec = opts ? opts->precision : MAFM_FP32C;
+        if (prec != MAFM_FP32C && prec != MAFM_DF)
+            fail(MAFM_E_UNSUPPORTED, "batched runs use MAFM_FP32C or MAFM_DF");
         if (opts && (opts->col_begin || opts->col_end))
             fail(MAFM_E_INVALID, "column ranges are per scan; batches relax whole scans");
+        const bool dfp = prec == MAFM_DF;
         cudaStream_t st = (cudaStream_t)stream;
         mafm_scan* s0 = scans[0];
         if (!s0) fail(MAFM_E_INVALID, "null scan in batch");
@@ -859,7 +924,8 @@ int mafm_run_batch(mafm_scan* const* scans, int32_t n_scans, const mafm_run_opts
             total_pts += (size_t)cols * s->d.nz;
             max_cols = std::max(max_cols, cols);
             total_cols += cols;
-            ensure_grid(*s, false, st);
+            if (dfp) check_df_supported(*s);
+            else ensure_grid(*s, false, st);
             ensure_order(*s, st);
             max_terms = std::max(max_terms, s->d.rigidgrid ? 0 : s->P.n_terms);
         }
@@ -890,9 +956,32 @@ int mafm_run_batch(mafm_scan* const* scans, int32_t n_scans, const mafm_run_opts
         dbs.alloc(bs.size());
         cuda_check(cudaMemcpyAsync(dbs.p, bs.data(), bs.size() * sizeof(BatchScan), cudaMemcpyHostToDevice, st),
                    "upload batch");
+        DevBuf<BatchDF> dbd;
+        DevBuf<unsigned long long> rlist;
+        if (dfp) {
+            std::vector<BatchDF> bd((size_t)n_scans);
+            long long first = 0;
+            for (int i = 0; i < n_scans; ++i) {
+                bd[i] = batch_df_entry(*scans[i], bs[i].out, 0, bs[i].col_end, true, first);
+                first += bs[i].col_end;
+            }
+            dbd.alloc(bd.size());
+            cuda_check(cudaMemcpyAsync(dbd.p, bd.data(), bd.size() * sizeof(BatchDF),
+                                       cudaMemcpyHostToDevice, st), "upload batch");
+            rlist.alloc((size_t)total_cols);
+            // the descriptors must reach the device before the host vector goes
+            cuda_check(cudaStreamSynchronize(st), "upload batch");
+        }
         zero_counters(*s0, st);
         cuda_check(cudaEventRecord(s0->ev0, st), "cudaEventRecord");
-        cuda_check(launch_relax32(dbs.p, n_scans, tiles, cfg, s0->ctr.p, st), "relax32 batch launch");
+        if (dfp) {
+            cuda_check(launch_relaxdf(dbd.p, n_scans, total_cols, s0->ctr.p, rlist.p, (unsigned)total_cols,
+                                      watchdog_ns_from_env(), st), "double-float relax launch");
+            cuda_check(launch_repair64(dbs.p, rlist.p, (unsigned)total_cols, -1, true, false, s0->ctr.p, st),
+                       "FP64 re-relaxation launch");
+        } else {
+            cuda_check(launch_relax32(dbs.p, n_scans, tiles, cfg, s0->ctr.p, st), "relax32 batch launch");
+        }
         cuda_check(cudaEventRecord(s0->ev1, st), "cudaEventRecord");
         if (host_out)
             for (int i = 0; i < n_scans; ++i) {
@@ -912,7 +1001,72 @@ int mafm_run_batch(mafm_scan* const* scans, int32_t n_scans, const mafm_run_opts
             stats->force_evals = c.force_evals;
             stats->pair_evals = c.pair_evals;
             stats->error_word = c.error_word;
-            stats->reserved = 0;
+            stats->fp64_columns = dfp ? (unsigned)std::min<long long>(c.n_tie, total_cols) : 0;
+            stats->kernel_ms = ms;
+        }
+        check_device_errors(c);
+    });
+}
+
+int mafm_run_columns(mafm_scan* scan, const int32_t* columns, int64_t n, mafm_point* out,
+                     mafm_run_stats* stats, void* stream) {
+    return guarded([&] {
+        if (!scan || (n > 0 && (!columns || !out))) fail(MAFM_E_INVALID, "null argument");
+        if (n < 0) fail(MAFM_E_INVALID, "negative column count");
+        if (stats) *stats = mafm_run_stats{};
+        if (n == 0) return;
+        const long long n_cols = (long long)scan->d.nx * scan->d.ny;
+        if (n > 0xffffffffll) fail(MAFM_E_RANGE, "more than 2^32 columns in one call");
+        std::vector<unsigned long long> list((size_t)n);
+        for (int64_t i = 0; i < n; ++i) {
+            if (columns[i] < 0 || columns[i] >= n_cols)
+                fail(MAFM_E_INVALID, "column %d outside [0, %lld)", columns[i], n_cols);
+            list[(size_t)i] = (unsigned long long)(unsigned)columns[i];
+        }
+        cuda_check(cudaSetDevice(scan->device), "cudaSetDevice");
+        cudaStream_t st = (cudaStream_t)stream;
+        const size_t n_pts = (size_t)n * scan->d.nz;
+        const bool host_out = !is_device_ptr(out);
+        mafm_point* const pinned = host_out ? pinned_view(out) : nullptr;
+        const bool staged = host_out && !pinned;
+        mafm_point* dout = pinned ? pinned : out;
+        if (staged) {
+            scan->stage.alloc(n_pts);
+            dout = scan->stage.p;
+        }
+        ensure_grid(*scan, true, st);
+        DevBuf<unsigned long long> dlist;
+        dlist.alloc((size_t)n);
+        cuda_check(cudaMemcpyAsync(dlist.p, list.data(), (size_t)n * sizeof(unsigned long long),
+                                   cudaMemcpyHostToDevice, st), "upload columns");
+        BatchScan b{};
+        b.p = build_params(*scan);
+        b.out = dout;
+        b.col_begin = 0;
+        b.col_end = (int)n_cols;
+        b.n_pairs_per_eval = scan->n_pairs_per_eval;
+        b.has_coulomb = scan->has_coulomb;
+        write_batch<<<1, 1, 0, st>>>(scan->batch.p, b);
+        cuda_check(cudaGetLastError(), "descriptor upload");
+        zero_counters(*scan, st);
+        cuda_check(cudaEventRecord(scan->ev0, st), "cudaEventRecord");
+        cuda_check(launch_repair64(scan->batch.p, dlist.p, (unsigned)n, n, false, true, scan->ctr.p, st),
+                   "FP64 column launch");
+        cuda_check(cudaEventRecord(scan->ev1, st), "cudaEventRecord");
+        if (staged)
+            cuda_check(cudaMemcpyAsync(out, dout, n_pts * sizeof(mafm_point), cudaMemcpyDeviceToHost, st),
+                       "copy points to host");
+        cuda_check(cudaMemcpyAsync(scan->host_ctr, scan->ctr.p, sizeof(RunCounters),
+                                   cudaMemcpyDeviceToHost, st), "copy counters");
+        cuda_check(cudaStreamSynchronize(st), "relax columns");
+        const RunCounters c = *scan->host_ctr;
+        if (stats) {
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, scan->ev0, scan->ev1);
+            stats->total_steps = c.total_steps;
+            stats->force_evals = c.force_evals;
+            stats->pair_evals = c.pair_evals;
+            stats->error_word = c.error_word;
             stats->kernel_ms = ms;
         }
         check_device_errors(c);
@@ -1031,6 +1185,11 @@ struct mafm_plan {
     mafm::Relax32Config cfg{};
     mafm::DevBuf<mafm::BatchScan> list;
     mafm::DevBuf<mafm::RunCounters> ctr;
+    // MAFM_DF: the double-float descriptors and the re-relaxation list
+    bool dfp = false;
+    long long cols = 0;
+    mafm::DevBuf<mafm::BatchDF> listdf;
+    mafm::DevBuf<unsigned long long> repair;
     mafm::RunCounters* host_ctr = nullptr;
     ~mafm_plan() {
         if (host_ctr) cudaFreeHost(host_ctr);
@@ -1056,8 +1215,10 @@ std::vector<BatchScan> batch_entries(mafm_scan* const* scans, int n, mafm_point*
 void plan_build(mafm_plan& p, mafm_scan* const* scans, int n, const mafm_run_opts* opts,
                 mafm_point* const* outs, cudaStream_t st) {
     if (!scans || !outs || n <= 0) fail(MAFM_E_INVALID, "empty batch");
-    if (opts && opts->precision != MAFM_FP32C) fail(MAFM_E_UNSUPPORTED, "plans run MAFM_FP32C");
+    const int prec = opts ? opts->precision : MAFM_FP32C;
+    if (prec != MAFM_FP32C && prec != MAFM_DF) fail(MAFM_E_UNSUPPORTED, "plans run MAFM_FP32C or MAFM_DF");
     if (opts && (opts->col_begin || opts->col_end)) fail(MAFM_E_INVALID, "plans relax whole scans");
+    p.dfp = prec == MAFM_DF;
     p.device = scans[0]->device;
     cuda_check(cudaSetDevice(p.device), "cudaSetDevice");
     long long cols = 0;
@@ -1066,7 +1227,8 @@ void plan_build(mafm_plan& p, mafm_scan* const* scans, int n, const mafm_run_opt
         if (!scans[i] || !outs[i]) fail(MAFM_E_INVALID, "null scan or output %d", i);
         if (scans[i]->device != p.device) fail(MAFM_E_INVALID, "scans of one plan must share a device");
         if (!is_device_ptr(outs[i])) fail(MAFM_E_INVALID, "plan outputs must be device memory");
-        ensure_grid(*scans[i], false, st);
+        if (p.dfp) check_df_supported(*scans[i]);
+        else ensure_grid(*scans[i], false, st);
         ensure_order(*scans[i], st);
         cols += (long long)scans[i]->d.nx * scans[i]->d.ny;
         max_terms = std::max(max_terms, scan_direct_terms(scans[i]));
@@ -1074,17 +1236,37 @@ void plan_build(mafm_plan& p, mafm_scan* const* scans, int n, const mafm_run_opt
     p.cfg = default_config(cols, max_terms, opts, n);
     std::vector<BatchScan> bs = batch_entries(scans, n, outs, p.cfg, p.tiles);
     p.n_scans = n;
+    p.cols = cols;
     p.list.alloc(bs.size());
     p.ctr.alloc(1);
     cuda_check(cudaMemcpyAsync(p.list.p, bs.data(), bs.size() * sizeof(BatchScan),
                                cudaMemcpyHostToDevice, st), "upload plan");
+    std::vector<BatchDF> bd;
+    if (p.dfp) {
+        long long first = 0;
+        for (int i = 0; i < n; ++i) {
+            bd.push_back(batch_df_entry(*scans[i], outs[i], 0, bs[i].col_end, true, first));
+            first += bs[i].col_end;
+        }
+        p.listdf.alloc(bd.size());
+        cuda_check(cudaMemcpyAsync(p.listdf.p, bd.data(), bd.size() * sizeof(BatchDF),
+                                   cudaMemcpyHostToDevice, st), "upload plan");
+        p.repair.alloc((size_t)cols);
+    }
     cuda_check(cudaStreamSynchronize(st), "upload plan");
     if (!p.host_ctr) cuda_check(cudaMallocHost(&p.host_ctr, sizeof(RunCounters)), "cudaMallocHost");
 }
 
 void plan_launch(mafm_plan& p, cudaStream_t st) {
     cuda_check(cudaMemsetAsync(p.ctr.p, 0, sizeof(RunCounters), st), "reset counters");
-    cuda_check(launch_relax32(p.list.p, p.n_scans, p.tiles, p.cfg, p.ctr.p, st), "relax32 launch");
+    if (p.dfp) {
+        cuda_check(launch_relaxdf(p.listdf.p, p.n_scans, p.cols, p.ctr.p, p.repair.p,
+                                  (unsigned)p.cols, p.cfg.watchdog_ns, st), "double-float relax launch");
+        cuda_check(launch_repair64(p.list.p, p.repair.p, (unsigned)p.cols, -1, true, false, p.ctr.p, st),
+                   "FP64 re-relaxation launch");
+    } else {
+        cuda_check(launch_relax32(p.list.p, p.n_scans, p.tiles, p.cfg, p.ctr.p, st), "relax32 launch");
+    }
 }
 
 }  // namespace
@@ -1128,6 +1310,7 @@ int mafm_plan_stats(mafm_plan* plan, mafm_run_stats* stats, void* stream) {
         stats->force_evals = c.force_evals;
         stats->pair_evals = c.pair_evals;
         stats->error_word = c.error_word;
+        stats->fp64_columns = plan->dfp ? (unsigned)std::min<long long>(c.n_tie, plan->cols) : 0;
         check_device_errors(c);
     });
 }
@@ -1144,7 +1327,7 @@ int mafm_plan_config(const mafm_plan* plan, mafm_run_opts* opts) {
     return guarded([&] {
         if (!plan || !opts) fail(MAFM_E_INVALID, "null argument");
         *opts = mafm_run_opts{};
-        opts->precision = MAFM_FP32C;
+        opts->precision = plan->dfp ? MAFM_DF : MAFM_FP32C;
         opts->lanes_per_column = plan->cfg.lanes;
         opts->block_threads = plan->cfg.block;
         opts->columns_per_tile = plan->cfg.cols_per_tile;

@@ -229,6 +229,16 @@ class Scan:
         check(lib().mafm_run(self._h, C.byref(o), ptr(out), C.byref(stats), stream))
         return out, stats
 
+    def run_columns(self, columns, stream=None):
+        """Plain FP64 relaxation of the listed columns (i * ny + j); returns
+        (points, stats) with column columns[m] at points[m*nz:(m+1)*nz]."""
+        cols = np.ascontiguousarray(columns, dtype=np.int32)
+        out = np.zeros(len(cols) * self.desc.c.nz, dtype=_abi.POINT_DTYPE)
+        stats = _abi.RunStats()
+        check(lib().mafm_run_columns(self._h, ptr(cols), len(cols), ptr(out), C.byref(stats),
+                                     stream))
+        return out, stats
+
     def run_device(self, out_ptr: int, precision=_abi.FP32C, lanes=0, block=0, tile=0,
                    stream=None, stats: bool = False):
         """Relax into device memory at out_ptr (no copy back).  stats=True synchronises."""

@@ -44,7 +44,10 @@ class _FzImage(torch.autograd.Function):
     @staticmethod
     def backward(ctx, grad_fz):
         w = grad_fz.detach().double().cpu().numpy().reshape(-1)
-        g = ctx.scan.adjoint(ctx.pts, w, precision=ctx.precision)
+        # a double-float forward differentiates with the FP32C adjoint (within
+        # 1e-5 of the FP64 one); the others in their own precision
+        prec = _abi.FP32C if ctx.precision == _abi.DF else ctx.precision
+        g = ctx.scan.adjoint(ctx.pts, w, precision=prec)
         out = []
         for key, shape, dt, dev in zip(("dpos", "dcharge", "dpair"), ctx.shapes, ctx.dtypes,
                                        ctx.devices):

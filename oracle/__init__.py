@@ -47,6 +47,9 @@ def port():
         L.oracle_run.restype = C.c_int
         L.oracle_run.argtypes = [C.POINTER(_abi.ScanDesc), C.c_int, C.c_int, C.c_void_p,
                                  C.c_int, C.POINTER(C.c_uint64)]
+        L.oracle_run_columns.restype = C.c_int
+        L.oracle_run_columns.argtypes = [C.POINTER(_abi.ScanDesc), C.c_void_p, C.c_int64,
+                                         C.c_void_p, C.c_int, C.POINTER(C.c_uint64)]
         L.oracle_run_split.restype = C.c_int
         L.oracle_run_split.argtypes = [C.POINTER(_abi.ScanDesc), C.c_int, C.c_int, C.c_void_p,
                                        C.c_int, C.POINTER(C.c_uint64), C.c_double * 2]
@@ -84,6 +87,21 @@ def run(desc, col_begin: int = 0, col_end: int | None = None, threads: int = 0):
     steps = C.c_uint64(0)
     _check(port().oracle_run(C.byref(d), col_begin, col_end, out.ctypes.data_as(C.c_void_p),
                              threads, C.byref(steps)))
+    return out, int(steps.value)
+
+
+def run_columns(desc, columns, threads: int = 0):
+    """Relax the listed columns (i * ny + j) with the FP64 port; returns
+    (points, total_steps) with column columns[i] at points[i*nz:(i+1)*nz]."""
+    from mechafm_gb300 import _abi
+    d = desc.c
+    cols = np.ascontiguousarray(columns, dtype=np.int32)
+    if len(cols) and (cols.min() < 0 or cols.max() >= d.nx * d.ny):
+        raise ValueError("column outside the scan")
+    out = np.zeros(len(cols) * d.nz, dtype=_abi.POINT_DTYPE)
+    steps = C.c_uint64(0)
+    _check(port().oracle_run_columns(C.byref(d), cols.ctypes.data_as(C.c_void_p), len(cols),
+                                     out.ctypes.data_as(C.c_void_p), threads, C.byref(steps)))
     return out, int(steps.value)
 
 
@@ -157,6 +175,21 @@ REF_FIELDS = ["i", "j", "k", "steps", "tip_x", "tip_y", "tip_z", "dum_x", "dum_y
 
 def ref_available() -> bool:
     return os.path.exists(REF_DUMP)
+
+
+def ref_time_columns(input_file: str, columns, tmp_prefix: str, threads: int = 0):
+    """The reference's own relaxation of the listed columns, timed inside
+    ref_dump (OpenMP over columns): returns (points, wall_s, total_steps)."""
+    cols = np.ascontiguousarray(columns, dtype=np.int32)
+    path = tmp_prefix + "_cols.bin"
+    cols.tofile(path)
+    env = dict(os.environ)
+    if threads > 0:
+        env["OMP_NUM_THREADS"] = str(threads)
+    r = subprocess.run([REF_DUMP, "time_cols", os.path.abspath(input_file), path], check=True,
+                       capture_output=True, text=True, env=env)
+    last = [l for l in r.stdout.splitlines() if l.startswith("points ")][-1].split()
+    return int(last[1]), float(last[3]), int(last[5])
 
 
 def ref_scan(input_file: str, out_bin: str, i_range=None, j_range=None) -> np.ndarray:

@@ -700,6 +700,25 @@ int oracle_run(const mafm_scan_desc* d, int col_begin, int col_end, mafm_point* 
     return 0;
 }
 
+/* oracle_run over a list of columns: out[i*nz + k] for column cols[i] (a
+ * seeded sample of pixels spread over the whole scan). */
+int oracle_run_columns(const mafm_scan_desc* d, const int32_t* cols, int64_t n, mafm_point* out,
+                       int nthreads, uint64_t* total_steps) {
+    Ctx c;
+    int st = ctx_init(&c, d);
+    if (st) { ctx_free(&c); return st; }
+    unsigned long long steps = 0;
+#pragma omp parallel for schedule(dynamic, 1) reduction(+ : steps) num_threads(nthreads > 0 ? nthreads : omp_get_max_threads())
+    for (int64_t i = 0; i < n; ++i) {
+        mafm_point* o = out + (size_t)i * d->nz;
+        column(&c, cols[i], o);
+        for (int k = 0; k < d->nz; ++k) steps += (unsigned long long)o[k].steps;
+    }
+    if (total_steps) *total_steps = steps;
+    ctx_free(&c);
+    return 0;
+}
+
 /* oracle_run with its wall time split into the set-up (terms, external field,
  * rigid grid: ctx_init) and the relaxation: t[0], t[1] in seconds. */
 int oracle_run_split(const mafm_scan_desc* d, int col_begin, int col_end, mafm_point* out,

@@ -18,6 +18,7 @@
 //   ref_dump sample_ts INPUT POINTS.bin OUT.bin   tip-surface F,E at given tip positions
 //   ref_dump sample_es INPUT POINTS.bin OUT.bin   external-field F,E at given tip positions
 //   ref_dump time   INPUT                          full scan timed, OpenMP over columns
+//   ref_dump time_cols INPUT COLS.bin              the listed columns (int32 i*ny + j) timed
 #include <chrono>
 #include <cstdio>
 #include <cstdlib>
@@ -206,6 +207,28 @@ int main(int argc, char** argv) {
         }
         double dt = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
         printf("points %d wall_s %.4f steps %lu\n", np.x * np.y * np.z, dt, steps);
+        return 0;
+    }
+    if (mode == "time_cols") {
+        if (argc < 4) return 2;
+        std::vector<int> cols;
+        FILE* f = fopen(argv[3], "rb");
+        if (!f) return 2;
+        int c;
+        while (fread(&c, sizeof c, 1, f) == 1) cols.push_back(c);
+        fclose(f);
+        for (int col : cols)
+            if (col < 0 || col >= np.x * np.y) return 2;
+        unsigned long steps = 0;
+        auto t0 = std::chrono::steady_clock::now();
+#pragma omp parallel for schedule(dynamic, 1) reduction(+ : steps)
+        for (size_t m = 0; m < cols.size(); ++m) {
+            std::vector<double> r((size_t)np.z * 25);
+            column(sim, cols[m] / np.y, cols[m] % np.y, r.data());
+            for (int k = 0; k < np.z; ++k) steps += (unsigned long)r[(size_t)k * 25 + 3];
+        }
+        double dt = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        printf("points %zu wall_s %.4f steps %lu\n", cols.size() * (size_t)np.z, dt, steps);
         return 0;
     }
     fprintf(stderr, "unknown mode %s\n", mode.c_str());
