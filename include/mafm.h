@@ -419,6 +419,19 @@ int mafm_scan_build_grid(mafm_scan* scan, int32_t precision, void* stream);
  * must end in '/' otherwise.  Rows are written in point order. */
 int mafm_write_output(const mafm_input* in, const mafm_point* pts, const char* folder,
                       int32_t gzip);
+/* The same files written chunk by chunk, so that a caller can format and
+ * write the points of one chunk of pixel columns while the GPU relaxes the
+ * next (the reference writes each height file as its buffer fills,
+ * simulation.cpp:123-138).  mafm_writer_open opens every height file;
+ * mafm_writer_append writes columns [col_begin, col_end) (c = i*ny + j),
+ * whose points pts holds at (c - col_begin)*nz + k (host memory); the ranges
+ * must follow one another from column 0, so the files receive their rows in
+ * pixel order and end up byte-identical to mafm_write_output's.
+ * mafm_writer_close closes them (and waits for gzip). */
+typedef struct mafm_writer mafm_writer;
+int mafm_writer_open(const mafm_input* in, const char* folder, int32_t gzip, mafm_writer** out);
+int mafm_writer_append(mafm_writer* w, const mafm_point* pts, int32_t col_begin, int32_t col_end);
+int mafm_writer_close(mafm_writer* w);
 /* System::makeXYZFile (system.cpp:54-66) for every height of one column of
  * a flexible scan: writes <folder>state_<x>-<y>-<z>.xyz (%.1f each: the pixel
  * position and the dummy height) with every atom's type and position, and

@@ -149,6 +149,9 @@ SIGNATURES = {
     "mafm_scan_grid_copy": (C.c_int, [_P, C.c_int32, _P]),
     "mafm_scan_build_grid": (C.c_int, [_P, C.c_int32, _P]),
     "mafm_write_output": (C.c_int, [_P, _P, C.c_char_p, C.c_int32]),
+    "mafm_writer_open": (C.c_int, [_P, C.c_char_p, C.c_int32, C.POINTER(_P)]),
+    "mafm_writer_append": (C.c_int, [_P, _P, C.c_int32, C.c_int32]),
+    "mafm_writer_close": (C.c_int, [_P]),
     "mafm_write_statistics": (C.c_int, [_P, C.c_char_p, C.c_uint64, C.c_double, C.c_double]),
 }
 

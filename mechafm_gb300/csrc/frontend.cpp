@@ -1002,8 +1002,11 @@ char* put_int(char* o, long long v) {
     return o;
 }
 
-void write_rows(const mafm_input& in, const mafm_point* pts, int k, FILE* f) {
-    const int nx = in.np[0], ny = in.np[1], nz = in.np[2];
+// Rows of height k for pixel columns [cb, ce) (c = i ny + j), in column
+// order; pts holds column c's points at (c - cb) nz + k.
+void write_rows(const mafm_input& in, const mafm_point* pts, int k, long long cb, long long ce,
+                FILE* f) {
+    const int ny = in.np[1], nz = in.np[2];
     // Dummy z after k calls of lowerTip (system.hpp:51-54).
     double dz_acc = in.zhigh;
     for (int s = 0; s < k; ++s) dz_acc -= in.dz;
@@ -1012,10 +1015,13 @@ void write_rows(const mafm_input& in, const mafm_point* pts, int k, FILE* f) {
     std::string buf;
     buf.reserve((size_t)ny * 120);
     char row[16 * kFieldMax];
-    for (int i = 0; i < nx; ++i) {
+    for (long long c0 = cb; c0 < ce;) {
+        // one x row (or the part of it inside the range) per buffer
+        const long long c1 = std::min(ce, (c0 / ny + 1) * ny);
         buf.clear();
-        for (int j = 0; j < ny; ++j) {
-            const mafm_point& p = pts[((size_t)i * ny + j) * nz + k];
+        for (long long c = c0; c < c1; ++c) {
+            const int i = (int)(c / ny), j = (int)(c % ny);
+            const mafm_point& p = pts[(size_t)(c - cb) * nz + k];
             const double x = i * in.dx, y = j * in.dy;
             double dxy[2] = {x, y};
             if (wrap) {
@@ -1050,6 +1056,7 @@ void write_rows(const mafm_input& in, const mafm_point* pts, int k, FILE* f) {
             buf.append(row, (size_t)(o - row));
         }
         fwrite(buf.data(), 1, buf.size(), f);
+        c0 = c1;
     }
 }
 
@@ -1182,32 +1189,85 @@ int mafm_input_free(mafm_input* in) {
     return MAFM_OK;
 }
 
-int mafm_write_output(const mafm_input* in, const mafm_point* pts, const char* folder,
-                      int32_t gzip) {
+// A scan's output files opened for appending rows in column order: each
+// scan-%06.3f.dat[.gz] file holds the rows of one height in pixel order
+// (simulation.cpp:145-199), so appending the columns of consecutive chunks
+// writes the same bytes as one call with every point.
+struct mafm_writer {
+    const mafm_input* in = nullptr;
+    bool gzip = false;
+    long long next_col = 0;
+    std::vector<FILE*> files;
+    void close_files() {
+        for (FILE*& f : files) {
+            if (!f) continue;
+            if (gzip) pclose(f);
+            else fclose(f);
+            f = nullptr;
+        }
+    }
+};
+
+int mafm_writer_open(const mafm_input* in, const char* folder, int32_t gzip, mafm_writer** out) {
     return mafm::guarded([&] {
-        if (!in || !pts || !folder) mafm::fail(MAFM_E_INVALID, "null argument");
+        if (!in || !folder || !out) mafm::fail(MAFM_E_INVALID, "null argument");
+        *out = nullptr;
+        auto* w = new mafm_writer();
+        w->in = in;
+        w->gzip = gzip != 0;
         const int nz = in->np[2];
-        std::vector<FILE*> files(nz, nullptr);
+        w->files.assign(nz, nullptr);
         char name[1024];
         for (int k = 0; k < nz; ++k) {
             const double z = in->zhigh - k * in->dz;
             if (gzip) {
                 snprintf(name, sizeof name, "gzip -6 > %sscan-%06.3f.dat.gz", folder, z);
-                files[k] = popen(name, "w");
+                w->files[k] = popen(name, "w");
             } else {
                 snprintf(name, sizeof name, "%sscan-%06.3f.dat", folder, z);
-                files[k] = fopen(name, "w");
+                w->files[k] = fopen(name, "w");
             }
-            if (!files[k]) mafm::fail(MAFM_E_IO, "cannot open %s", name);
+            if (!w->files[k]) {
+                w->close_files();
+                delete w;
+                mafm::fail(MAFM_E_IO, "cannot open %s", name);
+            }
         }
-        // One z-file per task; files are independent, so they are written in parallel.
-#pragma omp parallel for schedule(dynamic, 1)
-        for (int k = 0; k < nz; ++k) mafm::write_rows(*in, pts, k, files[k]);
-        for (int k = 0; k < nz; ++k) {
-            if (gzip) pclose(files[k]);
-            else fclose(files[k]);
-        }
+        *out = w;
     });
+}
+
+int mafm_writer_append(mafm_writer* w, const mafm_point* pts, int32_t col_begin, int32_t col_end) {
+    return mafm::guarded([&] {
+        if (!w || (!pts && col_end > col_begin)) mafm::fail(MAFM_E_INVALID, "null argument");
+        const long long n_cols = (long long)w->in->np[0] * w->in->np[1];
+        if (col_begin != w->next_col || col_end < col_begin || col_end > n_cols)
+            mafm::fail(MAFM_E_INVALID, "columns [%d, %d) do not continue the %lld written",
+                       col_begin, col_end, w->next_col);
+        const int nz = w->in->np[2];
+        // the height files are independent: formatted and written in parallel
+#pragma omp parallel for schedule(dynamic, 1)
+        for (int k = 0; k < nz; ++k)
+            mafm::write_rows(*w->in, pts, k, col_begin, col_end, w->files[k]);
+        w->next_col = col_end;
+    });
+}
+
+int mafm_writer_close(mafm_writer* w) {
+    if (!w) return MAFM_OK;
+    w->close_files();
+    delete w;
+    return MAFM_OK;
+}
+
+int mafm_write_output(const mafm_input* in, const mafm_point* pts, const char* folder,
+                      int32_t gzip) {
+    mafm_writer* w = nullptr;
+    int st = mafm_writer_open(in, folder, gzip, &w);
+    if (st != MAFM_OK) return st;
+    st = mafm_writer_append(w, pts, 0, in->np[0] * in->np[1]);
+    mafm_writer_close(w);
+    return st;
 }
 
 int mafm_write_states(const mafm_input* in, const double* states, int32_t column,

@@ -210,3 +210,51 @@ def test_fp32c_adjoint_matches_gpu_finite_differences(tmp_path):
         return float((w * p["force"][:, 2]).sum())
 
     fd_check(g, pert, loss)
+
+
+# ---- the adjoint at the C5 tolerance (ftol = etol = 0.01) ---------------------
+# The implicit adjoint differentiates the converged minimum F(x) = 0.  At the
+# C5 tolerance FIRE stops anywhere in |F| < 0.01, and a perturbation of any
+# size moves some point's stopping step, so the FIRE output is piecewise
+# smooth with jumps: its central differences do not converge as h shrinks
+# (measured on this 5 x 5 x 41 block: gaps to the implicit gradient of 3e-3
+# to 52x over h = 1e-1 ... 1e-5, not decreasing with h).  What the C5 gradient
+# can be held to is the exact gradient of the minima (the tight-tolerance
+# adjoint, itself within 1e-4 of finite differences): it differs from it by
+# the tolerance's own effect on the relaxed points, 0.2-3 % here.
+
+
+def c5_block(tmp, tight=False):
+    opts = {"minterm": "f", "ftol": "1e-10", "maxsteps": "400000"} if tight else {}
+    spec = synth.cluster_60(area=1.0, step=0.25, zhigh=10.0, zlow=6.0, **opts)
+    return Input(spec.write(str(tmp))).desc()
+
+
+def test_c5_tolerance_adjoint_is_within_5_percent_of_the_exact_gradient(tmp_path):
+    d_c5 = c5_block(tmp_path / "c5")
+    d_ex = c5_block(tmp_path / "tight", tight=True)
+    p_c5, _ = oracle.run(d_c5)
+    p_ex, _ = oracle.run(d_ex)
+    w = np.random.default_rng(3).normal(size=len(p_c5))
+    g_c5 = oracle.adjoint(d_c5, p_c5, w)
+    g_ex = oracle.adjoint(d_ex, p_ex, w)
+    for key in ("dpos", "dcharge"):
+        scale = np.abs(g_ex[key]).max()
+        err = np.abs(g_c5[key] - g_ex[key]).max() / scale
+        assert err <= 0.05, (key, err)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision,rel", [(_abi.FP64, 1e-9), (_abi.FP32C, 1e-5)])
+def test_gpu_adjoint_at_c5_tolerance_matches_oracle(tmp_path, precision, rel):
+    """On the C5-tolerance points (relaxed by the double-float kernel, which
+    takes FP64's steps), the GPU adjoint equals the oracle's adjoint."""
+    desc = c5_block(tmp_path)
+    scan = Scan(desc, device=0)
+    pts, _ = scan.run(_abi.DF)
+    w = np.random.default_rng(9).normal(size=len(pts))
+    g = scan.adjoint(pts, w, precision=precision)
+    want = oracle.adjoint(desc, pts, w)
+    for key in ("dpos", "dcharge", "dpair"):
+        scale = np.abs(want[key]).max()
+        np.testing.assert_allclose(g[key], want[key], rtol=0, atol=rel * scale)

@@ -1,0 +1,76 @@
+"""The external field at full size against the reference's kiss_fft.
+
+The 2048-atom periodic slab with its 160 x 160 x 120 Hartree cube (the
+bench's slab workload; radices 2^5 5 and 2^3 3 5, which take cuFFT down
+other paths than the 24-voxel fixtures): the seeded generator writes the
+input files again, their SHA-256 must equal the fixture's, then
+
+  * the FP64 field (cuFFT Z2Z) at 4000 seeded tip positions over the cell
+    equals the reference's (kiss_fft, ElectrostaticPotentialInteraction,
+    interactions.cpp:53-242) to 1e-9 of max(|F|, 0.01); the FP32 copy to 1e-4
+    (the FP32 lookup's fractional cell coordinates carry ~1e-6 of a 0.25 A
+    voxel);
+  * the relaxed points of the 8 x 8 pixel block over the rigid grid
+    (simulation.cpp:420-501): FP64 takes the reference's step count on at
+    least 99 % of the points (the grid and the field agree with the
+    reference's to rounding, so a FIRE decision may flip on a near-tie) with
+    the tip within 1e-6 A where it does; FP32C meets the metric's bar (tip
+    1e-3 A, Fz 1e-3 relative, floor 0.01) on at least 99 % of the points.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+from mechafm_gb300 import _abi
+from mechafm_gb300.scan import Input, Scan
+
+pytestmark = pytest.mark.gpu
+
+FOLDER = os.path.join(GOLDEN, "slab_c3")
+
+
+@pytest.fixture(scope="module")
+def c3(tmp_path_factory):
+    import sys
+    sys.path.insert(0, os.path.join(GOLDEN))
+    import make_c3_golden as g
+    meta = json.load(open(os.path.join(FOLDER, "meta.json")))
+    work = str(tmp_path_factory.mktemp("c3"))
+    inp = g.spec().write(work)
+    assert g.file_hashes(work) == meta["sha256"], "regenerated inputs differ from the fixture's"
+    ref = dict(np.load(os.path.join(FOLDER, "ref.npz")))
+    desc = Input(inp).desc()
+    scan = Scan(desc, device=0)
+    yield scan, ref
+    scan.close()
+
+
+@pytest.mark.parametrize("precision,tol", [(_abi.FP64, 1e-9), (_abi.FP32C, 1e-4)])
+def test_field_samples_match_kiss_fft(c3, precision, tol):
+    scan, ref = c3
+    fe = scan.sample(ref["es_pts"], precision=precision, what=1)
+    want = ref["es_fe"]
+    scale = np.maximum(np.abs(want), 1e-2)
+    err = np.abs(fe - want) / scale
+    assert err.max() <= tol, err.max()
+
+
+def test_block_fp64_matches_reference(c3):
+    scan, ref = c3
+    pts, _ = scan.run(_abi.FP64)
+    same = pts["steps"] == ref["steps"]
+    assert same.mean() >= 0.99, same.mean()
+    d = np.abs(pts["tip"] - ref["tip"]).max(axis=1)
+    assert d[same].max() <= 1e-6, d[same].max()
+
+
+def test_block_fp32c_within_bar(c3):
+    scan, ref = c3
+    pts, _ = scan.run(_abi.FP32C)
+    tip = np.abs(pts["tip"] - ref["tip"]).max(axis=1)
+    fz = np.abs(pts["force"][:, 2] - ref["force"][:, 2]) / np.maximum(np.abs(ref["force"][:, 2]), 0.01)
+    ok = (tip <= 1e-3) & (fz <= 1e-3)
+    assert ok.mean() >= 0.99, (ok.mean(), tip.max(), fz.max())

@@ -65,3 +65,37 @@ def test_state_files_match_reference_executable(tmp_path):
             got += [fn + "\t" + l.rstrip("\n") for l in open(os.path.join(tmp_path, fn))]
     want = open(os.path.join(folder, "cli_states.txt")).read().splitlines()
     assert got == want
+
+
+@pytest.mark.parametrize("use_gzip", [False, True])
+def test_chunked_writer_equals_one_shot_writer(use_gzip, tmp_path):
+    """mafm_writer_append over uneven column chunks (some ending inside a
+    pixel row) writes the same bytes as mafm_write_output, and refuses a
+    chunk that does not continue the columns written so far."""
+    import numpy as np
+    folder = os.path.join(GOLDEN, "cli_cluster")
+    inp = Input(os.path.join(folder, MANIFEST["cli_cluster"]["input"]))
+    desc = inp.desc()
+    pts, _ = oracle.run(desc)
+    one = tmp_path / "one"
+    chunked = tmp_path / "chunked"
+    one.mkdir()
+    chunked.mkdir()
+    inp.write_output(pts, str(one), gzip=use_gzip)
+    L = _abi.lib()
+    w = C.c_void_p()
+    _abi.check(L.mafm_writer_open(inp.handle, (str(chunked) + "/").encode(), int(use_gzip),
+                                  C.byref(w)))
+    n_cols, nz = desc.n_columns, desc.c.nz
+    cuts = sorted({0, n_cols, 1, n_cols // 3, n_cols // 3 + desc.c.ny + 1, n_cols - 2})
+    assert L.mafm_writer_append(w, pts.ctypes.data, 1, 2) == _abi.MAFM_E_INVALID
+    for a, b in zip(cuts[:-1], cuts[1:]):
+        chunk = np.ascontiguousarray(pts[a * nz:b * nz])
+        _abi.check(L.mafm_writer_append(w, chunk.ctypes.data, a, b))
+    L.mafm_writer_close(w)
+    names = sorted(os.listdir(one))
+    assert names == sorted(os.listdir(chunked)) and len(names) == nz
+    for fn in names:
+        opener = gzip.open if use_gzip else open
+        with opener(os.path.join(one, fn), "rb") as f1, opener(os.path.join(chunked, fn), "rb") as f2:
+            assert f1.read() == f2.read(), fn
