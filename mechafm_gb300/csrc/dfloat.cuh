@@ -122,16 +122,13 @@ __device__ __forceinline__ dfloat dfl_sqrt(dfloat a) {
 }
 
 // 1 / sqrt(a) for a > 0: one Newton step y (1 + (1 - a y^2) / 2) in
-// double-float from the FP32 approximation y
+// double-float from the FP32 approximation y, whose relative error e0 (about
+// 2^-23) leaves (3/2) e0^2, about 3e-14
 __device__ __forceinline__ dfloat dfl_rsqrt(dfloat a) {
     const float y = dfl_rsqrt_approx(a.h);
     const dfloat t = (a * y) * y;                        // about 1
     const float e = __fadd_rn(__fsub_rn(1.0f, t.h), -t.l);
-    const dfloat y1 = dfl_fast_two_sum(y, __fmul_rn(__fmul_rn(y, e), 0.5f));
-    // second step: the first correction carries the FP32 error of e's inputs
-    const dfloat t2 = (a * y1) * y1;
-    const float e2 = __fadd_rn(__fsub_rn(1.0f, t2.h), -t2.l);
-    return y1 + dfloat(__fmul_rn(__fmul_rn(y1.h, e2), 0.5f), 0.0f);
+    return dfl_fast_two_sum(y, __fmul_rn(__fmul_rn(y, e), 0.5f));
 }
 
 __device__ __forceinline__ bool operator<(dfloat a, dfloat b) {
