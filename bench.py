@@ -13,23 +13,28 @@ rebuilds the rigid grid and relaxes, as the reference does per scan) and
 adjoint_128 (the cluster at 128x128x41: forward relax + the implicit-
 differentiation adjoint of an MSE loss on the Fz image).
 
-One step = one relaxation of every point by the FP32-compensated persistent
-kernel, launched from a prepared plan (mafm_plan_launch) captured in a CUDA
-graph; launch shape (lanes per column, block, tile) from mafm_autotune.
-`value` = points/s with inputs resident and outputs in HBM; `e2e` = the same
-through the C ABI from host memory (scan creation with the upload, relax, and
-every point record delivered into pinned host memory).  The plain FP64 kernel runs on a subset for the FP32/FP64
-speed-up and the FP32C error against it.  The CPU baseline is the oracle port
-(FP64, OpenMP on every host thread) on a sample of about ten seconds: centre
-column blocks of every scan, or for rigid-grid scans a centre crop whose
-set-up, grid build and relaxation are timed apart and scaled to the full scan.
+One step = one relaxation of every point, launched from a prepared plan
+(mafm_plan_launch) captured in a CUDA graph.  The headline precision is
+MAFM_DF (double-float on the FP32 pipes, FP64's FIRE decisions, near-tie
+columns re-relaxed in FP64 inside the same step): its points meet the metric's
+1e-3 A / 1e-3 bar against FP64 on every point, which the run checks on all
+points of the scan (or a seeded uniform sample of columns of every scan when
+the scans hold more than FP64_FULL_POINTS).  Rigid-grid scans run MAFM_FP32C,
+which MAFM_DF does not cover.  MAFM_FP32C is also timed as the fast path, with
+its own error against FP64.  `value` = points/s with inputs resident and
+outputs in HBM; `e2e` = the same through the C ABI from host memory (scan
+creation with the upload, relax, every point record delivered into pinned host
+memory).  kernel_ms of the rooflines comes from events recorded inside the same
+graph replays that give ms_per_step.  The CPU baseline is the reference's own
+relaxation (oracle/_ref, where it was built) or the oracle port (FP64, OpenMP
+on every host thread) on a seeded uniform sample of pixel columns of about ten
+seconds.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
-                  [--workload NAME]
+                  [--workload NAME] [--precision df|fp32c]
   profiling knobs: --pixels P (a smaller scan), --lanes/--block/--tile
-  (a forced launch shape instead of the autotuner), --no-tune (the default
-  shape), --sweep (times lanes x block x tile shapes, to stderr),
-  --no-fp64 and --cpu-seconds 0 (skip the comparison legs).
+  (a forced FP32C launch shape instead of the autotuner), --no-tune (the
+  default shape), --no-fp64 and --cpu-seconds 0 (skip the comparison legs).
 """
 from __future__ import annotations
 
@@ -63,15 +68,15 @@ BYTES_LOOKUP = 8 * 16
 # 200 x 200 px slab launch: the grid nodes read once and the output records
 # written (gathers within a column are served by L1 and L2).
 DRAM_BYTES_PER_LOOKUP = 351.3e6 / 190890530
-# DRAM bytes (read + write) per relaxed point of relax32_kernel, from one ncu
-# capture of the cluster at 285 x 285 px x 41 z (171.9 MB for 3,330,225
-# points); the traffic is the 64 B output record per point, so it scales with
-# the points.
-DRAM_BYTES_PER_POINT = 171.9e6 / 3330225
+# Output bytes of one relaxed point (the 64 B mafm_point record); the relax
+# kernels' DRAM traffic is these records, written once.
+POINT_BYTES = 64
 CPU_TARGET_S = 10.0        # CPU sample length
 RIGID_CROP = 16            # pixels per side of the rigid-grid CPU sample
 FP64_RIGID_CROP = 64       # pixels per side of the rigid-grid FP64 comparison
 ADJ_CROP = 64              # pixels per side of the adjoint CPU sample
+FP64_FULL_POINTS = 8_000_000   # up to this many points FP64 relaxes every point
+FP64_SAMPLE_COLUMNS = 96       # else this many seeded columns per scan
 
 WORKLOADS = {
     "cluster_60": "60-atom C/N/O/H cluster, LJ+Morse+Coulomb, 401x401 px x 41 z",
@@ -91,16 +96,16 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="cluster_60", choices=sorted(WORKLOADS))
+    ap.add_argument("--precision", default="df", choices=["df", "fp32c"],
+                    help="headline precision (rigid-grid scans always run fp32c)")
     ap.add_argument("--cpu-seconds", type=float, default=CPU_TARGET_S,
                     help="length of the CPU sample (0 = skip the CPU baseline)")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-tune", action="store_true", help="default launch shape, no autotuner")
-    ap.add_argument("--lanes", type=int, default=0, help="force lanes per column")
-    ap.add_argument("--tile", type=int, default=0, help="force columns per tile")
-    ap.add_argument("--block", type=int, default=0, help="force threads per block")
+    ap.add_argument("--lanes", type=int, default=0, help="force FP32C lanes per column")
+    ap.add_argument("--tile", type=int, default=0, help="force FP32C columns per tile")
+    ap.add_argument("--block", type=int, default=0, help="force FP32C threads per block")
     ap.add_argument("--pixels", type=int, default=0, help="pixels per side (profiling)")
-    ap.add_argument("--sweep", action="store_true",
-                    help="also time every lanes-per-column value (stderr)")
     return ap.parse_args()
 
 
@@ -165,6 +170,13 @@ def centre_crop(desc, n: int):
     return desc.crop((d.nx - ni) // 2, (d.ny - nj) // 2, ni, nj)
 
 
+def sample_columns(n_columns: int, n: int, seed: int) -> np.ndarray:
+    """A seeded uniform sample of n pixel columns (i * ny + j) of a scan, sorted."""
+    rng = np.random.default_rng(seed)
+    n = min(n, n_columns)
+    return np.sort(rng.choice(n_columns, size=n, replace=False)).astype(np.int32)
+
+
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons while the timed region runs."""
 
@@ -223,46 +235,60 @@ def cpu_threads():
 
 # ------------------------------------------------------------ CPU baseline ----
 
-def _cpu_columns(descs, frac, threads):
-    """Relax the same centre fraction of every scan with the oracle port."""
+def _cpu_sample(inputs, descs, frac, threads, tmp):
+    """Relax a seeded uniform fraction of every scan's pixel columns on the
+    host: with the reference's own code (oracle/_ref/ref_dump, timed inside
+    it) where that was built, else with the oracle port.  Returns (points,
+    seconds, columns, kind)."""
     import oracle
+    use_ref = oracle.ref_available()
     jobs = []
-    for d in descs:
+    for i, (inp, d) in enumerate(zip(inputs, descs)):
         n = max(1, min(d.n_columns, int(round(frac * d.n_columns))))
-        c0 = max(0, d.n_columns // 2 - n // 2)
-        jobs.append((d, c0, c0 + n))
-    t0 = time.perf_counter()
-    if len(jobs) == 1:
-        d, a, b = jobs[0]
-        pts = len(oracle.run(d, a, b, threads=threads)[0])
+        jobs.append((inp, d, sample_columns(d.n_columns, n, 1000 + i)))
+    pts, wall = 0, 0.0
+    if use_ref:
+        for k, (inp, d, cols) in enumerate(jobs):
+            p, t, _ = oracle.ref_time_columns(inp.path, cols, os.path.join(tmp, f"cpu{k}"), threads)
+            pts += p
+            wall += t
+    elif len(jobs) == 1:
+        inp, d, cols = jobs[0]
+        t0 = time.perf_counter()
+        pts = len(oracle.run_columns(d, cols, threads=threads)[0])
+        wall = time.perf_counter() - t0
     else:
         # many scans: one scan per host thread (the port releases the GIL)
+        t0 = time.perf_counter()
         with ThreadPoolExecutor(threads) as ex:
-            pts = sum(ex.map(lambda j: len(oracle.run(j[0], j[1], j[2], threads=1)[0]), jobs))
-    return pts, time.perf_counter() - t0, sum(b - a for _, a, b in jobs)
+            pts = sum(ex.map(lambda j: len(oracle.run_columns(j[1], j[2], threads=1)[0]), jobs))
+        wall = time.perf_counter() - t0
+    return pts, wall, sum(len(c) for _, _, c in jobs), ("reference" if use_ref else "port")
 
 
-def cpu_direct(descs, threads, target_s):
-    """Points/s of the oracle over centre column blocks of every scan, sized to
-    about target_s seconds after a short pilot."""
+def cpu_direct(inputs, descs, threads, target_s, tmp):
+    """Points/s over a seeded uniform sample of the columns of every scan, sized
+    to about target_s seconds after a short pilot.  Returns (rate, text,
+    kind, seconds, points)."""
     total = sum(d.n_columns for d in descs)
     frac = min(1.0, 400.0 / total)
-    pts, t, cols = _cpu_columns(descs, frac, threads)
+    pts, t, cols, kind = _cpu_sample(inputs, descs, frac, threads, tmp)
     if t < target_s and frac < 1.0:
         frac = min(1.0, frac * target_s / max(t, 1e-3))
-        pts, t, cols = _cpu_columns(descs, frac, threads)
-    return pts / t, (f"{cols} centre columns x all z ({100 * frac:.2f}% of every scan), "
-                     f"{t:.1f} s")
+        pts, t, cols, kind = _cpu_sample(inputs, descs, frac, threads, tmp)
+    return pts / t, (f"{cols} seeded uniform columns x all z ({100 * frac:.2f}% of the columns "
+                     f"of every scan), {pts} points in {t:.1f} s"), kind, t, pts
 
 
 def cpu_rigid(descs, threads, crop_n):
     """Points/s of the oracle on rigid-grid scans, from a centre crop: the
     set-up (external field), the grid build and the relaxation are timed apart
-    and scaled to the full scan by grid nodes and by points."""
+    and scaled to the full scan by grid nodes and by points (a rigid grid spans
+    the whole scan area, so a sample of scattered columns would build it all)."""
     import oracle
     from mechafm_gb300 import _abi
     from mechafm_gb300.scan import Desc
-    est, pts, wall = 0.0, 0, 0.0
+    est, pts, wall, n_crop = 0.0, 0, 0.0, 0
     for desc in descs:
         crop = centre_crop(desc, crop_n)
         es = _abi.ScanDesc()
@@ -274,16 +300,17 @@ def cpu_rigid(descs, threads, crop_n):
         est += (t_es + t_grid * rigid_nodes(desc.c) / rigid_nodes(crop.c)
                 + t_relax * desc.n_points / len(out))
         pts += desc.n_points
+        n_crop += len(out)
         wall += t_es + t_setup + t_relax
-    return pts / est, (f"{crop_n}x{crop_n} centre crop of every scan ({wall:.1f} s): external "
-                       f"field, grid build (scaled by grid nodes) and relaxation (scaled by "
-                       f"points) timed apart")
+    return pts / est, (f"{crop_n}x{crop_n} centre crop of every scan ({n_crop} points, "
+                       f"{wall:.1f} s): external field, grid build (scaled by grid nodes) and "
+                       f"relaxation (scaled by points) timed apart"), "port", wall, n_crop
 
 
 def cpu_adjoint(descs, threads, crop_n):
     """Points/s of the oracle's forward relaxation + adjoint on a centre crop."""
     import oracle
-    rate, wall = [], 0.0
+    rate, wall, n_pts = [], 0.0, 0
     for desc in descs:
         crop = centre_crop(desc, crop_n)
         t0 = time.perf_counter()
@@ -293,22 +320,25 @@ def cpu_adjoint(descs, threads, crop_n):
         t = time.perf_counter() - t0
         rate.append(len(pts) / t)
         wall += t
+        n_pts += len(pts)
     return float(np.mean(rate)), (f"{crop_n}x{crop_n} centre crop, forward FP64 relaxation + "
-                                  f"adjoint, {wall:.1f} s")
+                                  f"adjoint, {wall:.1f} s"), "port", wall, n_pts
 
 
-def cpu_rate(kind, descs, threads, target_s):
+def cpu_rate(kind, inputs, descs, threads, target_s, tmp):
     if kind == "adjoint":
         return cpu_adjoint(descs, threads, ADJ_CROP)
     if any(d.c.rigidgrid for d in descs):
         return cpu_rigid(descs, threads, RIGID_CROP)
-    return cpu_direct(descs, threads, target_s)
+    return cpu_direct(inputs, descs, threads, target_s, tmp)
 
 
 def reference_arm(args, rank):
-    """--impl reference: the reference's CPU path (the oracle port of its FP64
-    OpenMP code; the reference's own build needs its sources, absent on the GPU
-    host), on all host threads, over a bounded sample of the same workload."""
+    """--impl reference: the reference's CPU path on all host threads over a
+    bounded sample of the same workload: the reference's own code
+    (oracle/_ref, built from its sources where they were present) or else the
+    oracle port of its FP64 OpenMP code.  ms_per_step is the time each step
+    actually took for its sample; value is the sample's points/s."""
     if rank != 0:
         return
     tmp = tempfile.mkdtemp()
@@ -317,20 +347,28 @@ def reference_arm(args, rank):
     threads = cpu_threads()
     kind = "adjoint" if args.workload == "adjoint_128" else "forward"
     for _ in range(args.warmup):
-        cpu_rate(kind, descs, threads, 0.5)
-    rates, sample = [], ""
+        cpu_rate(kind, inputs, descs, threads, 0.5, tmp)
+    rates, secs, pts = [], [], []
+    sample, arm = "", "port"
     for _ in range(args.steps):
-        r, sample = cpu_rate(kind, descs, threads, args.cpu_seconds or CPU_TARGET_S)
+        r, sample, arm, t, p = cpu_rate(kind, inputs, descs, threads,
+                                        args.cpu_seconds or CPU_TARGET_S, tmp)
         rates.append(r)
+        secs.append(t)
+        pts.append(p)
     value = float(np.mean(rates))
-    n_pts = sum(d.n_points for d in descs)
     print(json.dumps({
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": 1000.0 * n_pts / value, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": desc_text, "precision": "FP64 CPU (oracle port, OpenMP)"},
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+        "ms_per_step": 1000.0 * float(np.mean(secs)), "points_per_step": int(np.mean(pts)),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic",
+        "config": {"workload": desc_text,
+                   "precision": ("FP64 CPU, the reference's own code built from its sources "
+                                 "(oracle/_ref), OpenMP" if arm == "reference" else
+                                 "FP64 CPU (oracle port of the reference's code, OpenMP)"),
+                   "step": "a seeded sample of the workload (see cpu_baseline.sample)"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": arm,
                          "sample": sample + " per step; points/s of the sample"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }))
@@ -338,72 +376,63 @@ def reference_arm(args, rank):
 
 # ------------------------------------------------------------- GPU helpers ----
 
-def fp64_compare(scans, descs, value, dev):
-    """Plain FP64 kernel on a subset: points/s, and the FP32C error against it.
-    Rigid-grid scans are compared on a centre crop (both precisions build
-    their own grid of the crop; the FP64 time is the relaxation only)."""
-    import torch
+def err_stats(pts, ref):
+    """Tip and relative Fz error (denominator max(|Fz_ref|, 0.01 = ftol)) of
+    pts against ref, over every point."""
+    tip = np.abs(pts["tip"] - ref["tip"]).max(axis=1)
+    fz = np.abs(pts["force"][:, 2] - ref["force"][:, 2]) / np.maximum(np.abs(ref["force"][:, 2]), 0.01)
+    return {"tip_err_A": {"max": float(tip.max()), "p99_9": float(np.percentile(tip, 99.9)),
+                          "median": float(np.median(tip)),
+                          "frac_le_1e-3": float((tip <= 1e-3).mean())},
+            "fz_rel_err": {"max": float(fz.max()), "p99_9": float(np.percentile(fz, 99.9)),
+                           "frac_le_1e-3": float((fz <= 1e-3).mean())},
+            "points_beyond_bar": int(((tip > 1e-3) | (fz > 1e-3)).sum()),
+            "step_count_match": float((pts["steps"] == ref["steps"]).mean())}
+
+
+def fp64_reference(scans, descs, dev):
+    """FP64 points to check the other precisions against: every point of the
+    scans when they hold at most FP64_FULL_POINTS (the plain FP64 kernel,
+    mafm_run), else a seeded uniform sample of FP64_SAMPLE_COLUMNS columns of
+    every scan (mafm_run_columns, same bits).  Rigid-grid scans: a centre
+    crop (every precision builds its own grid of the crop).  Returns
+    (list of (scan, columns or None, points), points, kernel ms, text)."""
     from mechafm_gb300 import _abi
     from mechafm_gb300.scan import Scan
-    props = torch.cuda.get_device_properties(dev)
-    owned = []
-    if len(scans) == 1 and descs[0].c.rigidgrid:
-        s = Scan(centre_crop(descs[0], FP64_RIGID_CROP), device=dev)
-        owned.append(s)
-        jobs = [(s, 0, 0)]
-        subset = f"{FP64_RIGID_CROP}x{FP64_RIGID_CROP} centre crop"
-    elif len(scans) == 1:
-        d = descs[0]
-        cols = min(d.n_columns, props.multi_processor_count * 256)
-        c0 = d.n_columns // 2 - cols // 2
-        jobs = [(scans[0], c0, c0 + cols)]
-        subset = f"{cols} centre columns"
-    else:
-        jobs = [(s, 0, 0) for s in scans[:3]]
-        subset = "the first 3 scans"
-    p64s, p32s, ms64, npts = [], [], 0.0, 0
-    ms_build64 = 0.0
-    for s, a, b in jobs:
-        if s.desc.c.rigidgrid:
-            # the FP64 grid build of the crop, timed on its own
-            stream = torch.cuda.current_stream(dev)
-            sp = C.c_void_p(stream.cuda_stream)
-            _abi.check(_abi.lib().mafm_scan_build_grid(s.handle, _abi.FP64, sp))
-            ms_build64 = time_events(stream, lambda: _abi.check(
-                _abi.lib().mafm_scan_build_grid(s.handle, _abi.FP64, sp)))
-        p64, s64 = s.run(_abi.FP64, col_begin=a, col_end=b)
-        p32, _ = s.run(_abi.FP32C, col_begin=a, col_end=b)
-        p64s.append(p64)
-        p32s.append(p32)
-        ms64 += s64.kernel_ms
+    total = sum(d.n_points for d in descs)
+    refs, ms, npts = [], 0.0, 0
+    if any(d.c.rigidgrid for d in descs):
+        for s in scans:
+            crop = Scan(centre_crop(s.desc, FP64_RIGID_CROP), device=dev)
+            p64, st = crop.run(_abi.FP64)
+            refs.append((crop, None, p64))
+            ms += st.kernel_ms
+            npts += len(p64)
+        return refs, npts, ms, f"{FP64_RIGID_CROP}x{FP64_RIGID_CROP} centre crop, every point"
+    if total <= FP64_FULL_POINTS:
+        for s in scans:
+            p64, st = s.run(_abi.FP64)
+            refs.append((s, None, p64))
+            ms += st.kernel_ms
+            npts += len(p64)
+        return refs, npts, ms, "every point of the scan (relax64_kernel)"
+    for i, s in enumerate(scans):
+        cols = sample_columns(s.desc.n_columns, FP64_SAMPLE_COLUMNS, 2000 + i)
+        p64, st = s.run_columns(cols)
+        refs.append((s, cols, p64))
+        ms += st.kernel_ms
         npts += len(p64)
-    crop_nodes = rigid_nodes(owned[0].desc.c) if owned else 0
-    for s in owned:
-        s.close()
-    p64 = np.concatenate(p64s)
-    p32 = np.concatenate(p32s)
-    tip_err = np.abs(p32["tip"] - p64["tip"]).max(axis=1)
-    fz = np.abs(p32["force"][:, 2] - p64["force"][:, 2]) / np.maximum(np.abs(p64["force"][:, 2]), 0.01)
-    rate64 = npts / (ms64 / 1000.0)
-    extra = {}
-    if owned:
-        # a rigid-grid step is grid build + relax: scale the crop's FP64 build
-        # by grid nodes and its relax by points, as the FP32C step does both
-        d = descs[0]
-        t64 = (ms_build64 * rigid_nodes(d.c) / crop_nodes + ms64 * d.n_points / npts) / 1000.0
-        rate64 = d.n_points / t64
-        extra = {"grid_build_ms_crop": ms_build64, "relax_ms_crop": ms64,
-                 "scaled_to": "full scan: build by grid nodes, relax by points"}
-    return {
-        "points_per_s": rate64, "points": npts, "subset": subset, "kernel_ms": ms64, **extra,
-        "fp32c_speedup": value / rate64,
-        "tip_err_A": {"max": float(tip_err.max()), "p99_9": float(np.percentile(tip_err, 99.9)),
-                      "median": float(np.median(tip_err)),
-                      "frac_le_1e-3": float((tip_err <= 1e-3).mean())},
-        "fz_rel_err": {"max": float(fz.max()), "p99_9": float(np.percentile(fz, 99.9)),
-                       "frac_le_1e-3": float((fz <= 1e-3).mean())},
-        "step_count_match": float((p32["steps"] == p64["steps"]).mean()),
-    }
+    return refs, npts, ms, (f"{FP64_SAMPLE_COLUMNS} seeded uniform columns x all z of each of the "
+                            f"{len(scans)} scans (mafm_run_columns, one warp per column, the bits "
+                            f"of relax64_kernel)")
+
+
+def pick(points, cols, nz):
+    """The points of the listed columns from a whole-scan array."""
+    if cols is None:
+        return points
+    idx = (cols[:, None].astype(np.int64) * nz + np.arange(nz)[None, :]).reshape(-1)
+    return points[idx]
 
 
 def fp32_peak(dev):
@@ -437,21 +466,6 @@ def hbm_peak():
         return 6800.0, "fallback 6.8 TB/s"
 
 
-def time_events(stream, fn, reps=1):
-    """Mean ms of fn() on the stream, CUDA events around each call."""
-    import torch
-    ts = []
-    for _ in range(reps):
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        fn()
-        e1.record(stream)
-        torch.cuda.synchronize()
-        ts.append(e0.elapsed_time(e1))
-    return float(np.mean(ts))
-
-
 def job_ms(times, world, device):
     """Mean step time of this rank, then the maximum over ranks (every rank
     relaxes its own replica; the job ends with the slowest)."""
@@ -479,6 +493,70 @@ def fp32_roofline(achieved, peak, extra):
     return r
 
 
+def timing_event(external):
+    import torch
+    if external:
+        return torch.cuda.Event(enable_timing=True, external=True)
+    return torch.cuda.Event(enable_timing=True)
+
+
+def external_events_work(stream) -> bool:
+    """Whether this PyTorch records timing events inside a captured graph
+    (external event-record nodes): probed on a throwaway graph."""
+    import torch
+    try:
+        x = torch.zeros(16, device=stream.device)
+        a, b = timing_event(True), timing_event(True)
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g, stream=stream):
+            a.record(stream)
+            x.add_(1.0)
+            b.record(stream)
+        g.replay()
+        torch.cuda.synchronize()
+        a.elapsed_time(b)
+        return True
+    except Exception:
+        torch.cuda.synchronize()
+        return False
+
+
+class GraphStep:
+    """One step captured in a CUDA graph, with events recorded inside the
+    graph around each part (external event-record nodes), so that the parts'
+    device times come from the same replays as the step time.  Where the
+    PyTorch build lacks external events, the parts are timed by events around
+    plain launches of the same replays instead."""
+
+    def __init__(self, stream, parts):
+        import torch
+        self.stream = stream
+        self.parts = parts          # [(name, fn)]
+        self.graph = torch.cuda.CUDAGraph()
+        self.external = external_events_work(stream)
+        self.ev = [timing_event(self.external) for _ in range(len(parts) + 1)]
+        with torch.cuda.graph(self.graph, stream=stream):
+            if self.external:
+                self.ev[0].record(stream)
+            for k, (_, fn) in enumerate(self.parts):
+                fn()
+                if self.external:
+                    self.ev[k + 1].record(stream)
+
+    def replay(self):
+        """Replay the step on the stream (the caller synchronises)."""
+        if self.external:
+            self.graph.replay()
+        else:
+            self.ev[0].record(self.stream)
+            for k, (_, fn) in enumerate(self.parts):
+                fn()
+                self.ev[k + 1].record(self.stream)
+
+    def part_ms(self):
+        return {name: self.ev[k].elapsed_time(self.ev[k + 1]) for k, (name, _) in enumerate(self.parts)}
+
+
 # --------------------------------------------------------------- our arm -----
 
 def ours(args, rank, world, local):
@@ -501,14 +579,22 @@ def ours(args, rank, world, local):
     torch.cuda.synchronize()
     t_create = time.perf_counter() - t_create
     n_pts = sum(d.n_points for d in descs)
-    outs = [torch.empty(d.n_points * 64, dtype=torch.uint8, device=f"cuda:{dev}") for d in descs]
+    nz = descs[0].c.nz
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=f"cuda:{dev}")
     stream = torch.cuda.Stream(device=dev)
     sptr = C.c_void_p(stream.cuda_stream)
     n = len(scans)
     handles = (C.c_void_p * n)(*[s.handle for s in scans])
-    optrs = (C.c_void_p * n)(*[o.data_ptr() for o in outs])
     rigid = [s for s in scans if s.desc.c.rigidgrid]
+    head = _abi.DF if (args.precision == "df" and not rigid) else _abi.FP32C
+    head_name = "DF" if head == _abi.DF else "FP32C"
+
+    def device_outs():
+        bufs = [torch.empty(d.n_points * 64, dtype=torch.uint8, device=f"cuda:{dev}") for d in descs]
+        return bufs, (C.c_void_p * n)(*[o.data_ptr() for o in bufs])
+
+    def host_points(bufs):
+        return [np.frombuffer(b.cpu().numpy().tobytes(), dtype=_abi.POINT_DTYPE) for b in bufs]
 
     # Rigid grids: the first build allocates (outside the timing); a step rebuilds.
     t_grid = 0.0
@@ -519,17 +605,24 @@ def ours(args, rank, world, local):
         torch.cuda.synchronize()
         t_grid = time.perf_counter() - t0
 
-    # launch shape: the autotuner (its sweep on the first 32 scans of a batch,
-    # then the winner against the default shape on all of them)
-    opts = _abi.RunOpts(_abi.FP32C, args.lanes, args.block, args.tile, 0, 0)
+    # FP32C launch shape: the autotuner (its sweep on the first 32 scans of a
+    # batch, then the winner against the default shape on all of them)
+    opts32 = _abi.RunOpts(_abi.FP32C, args.lanes, args.block, args.tile, 0, 0)
     tune_ms = None
     if not args.no_tune and not (args.lanes or args.block or args.tile):
         best = _abi.RunOpts()
         tms = C.c_double()
         _abi.check(L.mafm_autotune(handles, n, C.byref(best), C.byref(tms), sptr))
-        opts, tune_ms = best, tms.value
-    plan = C.c_void_p()
-    _abi.check(L.mafm_plan_create(handles, n, C.byref(opts), optrs, C.byref(plan)))
+        opts32, tune_ms = best, tms.value
+
+    def make_plan(prec, bufs_ptrs):
+        o = opts32 if prec == _abi.FP32C else _abi.RunOpts(prec, 0, 0, 0, 0, 0)
+        plan = C.c_void_p()
+        _abi.check(L.mafm_plan_create(handles, n, C.byref(o), bufs_ptrs, C.byref(plan)))
+        return plan
+
+    outs, optrs = device_outs()
+    plan = make_plan(head, optrs)
     used = _abi.RunOpts()
     _abi.check(L.mafm_plan_config(plan, C.byref(used)))
 
@@ -559,7 +652,7 @@ def ours(args, rank, world, local):
                 pair[t, 2] *= us[t]
         dt_ = d0.with_terms(a["pos"] + rng.normal(0, 0.05, size=a["pos"].shape), a["charge"], pair)
         st_ = Scan(dt_, device=dev)
-        tp, _ = st_.run(_abi.FP32C)
+        tp, _ = st_.run(head)
         st_.close()
         target = torch.from_numpy(tp["force"][:, 2].copy()).to(f"cuda:{dev}")
         fz_view = outs[0].view(torch.float64).view(-1, 8)[:, 5]
@@ -578,20 +671,20 @@ def ours(args, rank, world, local):
             _abi.check(L.mafm_adjoint_ex(scans[0].handle, _abi.FP32C, C.c_void_p(outs[0].data_ptr()),
                                          C.c_void_p(wbuf.data_ptr()), C.byref(grads), sptr))
 
+    parts = ([("grid_build", build)] if rigid else []) + [("relax", relax)]
     for _ in range(args.warmup):
-        build()
-        relax()
+        for _, fn in parts:
+            fn()
         if adjoint:
             adj()
     st = _abi.RunStats()
     _abi.check(L.mafm_plan_stats(plan, C.byref(st), sptr))
-    graph = torch.cuda.CUDAGraph()
-    with torch.cuda.graph(graph, stream=stream):
-        build()
-        relax()
+    step = GraphStep(stream, parts)
     torch.cuda.synchronize()
 
-    times = []
+    times, part_times = [], {name: [] for name, _ in parts}
+    if adjoint:
+        part_times["adjoint"] = []
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
@@ -601,34 +694,59 @@ def ours(args, rank, world, local):
                 flush.zero_()
                 e0 = torch.cuda.Event(enable_timing=True)
                 e1 = torch.cuda.Event(enable_timing=True)
+                ea = torch.cuda.Event(enable_timing=True)
                 e0.record(stream)
-                graph.replay()
+                step.replay()
+                ea.record(stream)
                 if adjoint:
                     adj()
                 e1.record(stream)
             torch.cuda.synchronize()
             times.append(e0.elapsed_time(e1))
+            for name, v in step.part_ms().items():
+                part_times[name].append(v)
+            if adjoint:
+                part_times["adjoint"].append(ea.elapsed_time(e1))
     ms = job_ms(times, world, f"cuda:{dev}")
     value = replica_throughput(n_pts, world, ms)
     _abi.check(L.mafm_plan_stats(plan, C.byref(st), sptr))   # the last replay ended cleanly
+    ms_part = {k: float(np.mean(v)) for k, v in part_times.items()}
 
-    # the kernels apart, for the rooflines
-    ms_relax = time_events(stream, relax, 2)
-    ms_build = time_events(stream, build, 2) if rigid else 0.0
-    ms_adj = time_events(stream, adj, 2) if adjoint else 0.0
+    # the fast path (FP32C) timed the same way, when the headline is DF
+    fast = None
+    outs32 = None
+    if head == _abi.DF:
+        outs32, optrs32 = device_outs()
+        plan32 = make_plan(_abi.FP32C, optrs32)
 
-    if args.sweep and rank == 0:
-        for lanes in (1, 2, 4, 8):
-            for block in (128, 256):
-                for tile in sorted({1, 2, 4, 8, 32 // lanes, 128 // lanes}):
-                    o = _abi.RunOpts(_abi.FP32C, lanes, block, tile, 0, 0)
-                    p2 = C.c_void_p()
-                    _abi.check(L.mafm_plan_create(handles, n, C.byref(o), optrs, C.byref(p2)))
-                    _abi.check(L.mafm_plan_launch(p2, sptr))
-                    t = time_events(stream, lambda: _abi.check(L.mafm_plan_launch(p2, sptr)), 2)
-                    L.mafm_plan_destroy(p2)
-                    print(json.dumps({"sweep_lanes": lanes, "block": block, "tile": tile, "ms": t,
-                                      "points_per_s": n_pts / t * 1e3}), file=sys.stderr)
+        def relax32():
+            _abi.check(L.mafm_plan_launch(plan32, sptr))
+
+        for _ in range(args.warmup):
+            relax32()
+        step32 = GraphStep(stream, [("relax", relax32)])
+        t32 = []
+        for _ in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.zero_()
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                step32.replay()
+                e1.record(stream)
+            torch.cuda.synchronize()
+            t32.append(e0.elapsed_time(e1))
+        st32 = _abi.RunStats()
+        _abi.check(L.mafm_plan_stats(plan32, C.byref(st32), sptr))
+        ms32 = job_ms(t32, world, f"cuda:{dev}")
+        used32 = _abi.RunOpts()
+        _abi.check(L.mafm_plan_config(plan32, C.byref(used32)))
+        fast = {"precision": "FP32C", "points_per_s": replica_throughput(n_pts, world, ms32),
+                "ms_per_step": ms32, "force_evals": int(st32.force_evals),
+                "launch": {"lanes_per_column": used32.lanes_per_column,
+                           "block_threads": used32.block_threads,
+                           "columns_per_tile": used32.columns_per_tile}}
+        L.mafm_plan_destroy(plan32)
 
     # e2e through the public API from host memory
     h2d = 0
@@ -639,8 +757,8 @@ def ours(args, rank, world, local):
     e2e_times = []
     reps = 2 if n == 1 else 1
     if adjoint:
-        # torch.autograd through fz_image: scan creation, FP32C relax, D2H of
-        # the points, loss, backward = mafm_adjoint (points and dL/dFz uploaded)
+        # torch.autograd through fz_image: scan creation, relax, D2H of the
+        # points, loss, backward = mafm_adjoint (points and dL/dFz uploaded)
         from mechafm_gb300.torch_ops import fz_image
         d0 = descs[0]
         a = d0.atoms()
@@ -651,7 +769,7 @@ def ours(args, rank, world, local):
             pos = torch.tensor(a["pos"], requires_grad=True)
             chg = torch.tensor(a["charge"], requires_grad=True)
             pr = torch.tensor(d0.pair_params(), requires_grad=True)
-            fz = fz_image(d0, pos, chg, pr, precision=_abi.FP32C, device=dev)
+            fz = fz_image(d0, pos, chg, pr, precision=head, device=dev)
             loss = ((fz - tgt) ** 2).mean()
             loss.backward()
             if i > 0:
@@ -659,11 +777,12 @@ def ours(args, rank, world, local):
         h2d += n_pts * (64 + 8)
         d2h = n_pts * 64
     else:
-        # pinned host buffers for the results (written by the kernel directly)
+        # pinned host buffers for the results (written by the kernels directly)
         pinned = [torch.empty(d.n_points * 64, dtype=torch.uint8, pin_memory=True) for d in descs]
         host = [p.numpy().view(_abi.POINT_DTYPE) for p in pinned]
-        e2e_opts = _abi.RunOpts(_abi.FP32C, used.lanes_per_column, used.block_threads,
-                                used.columns_per_tile, 0, 0)
+        e2e_opts = (_abi.RunOpts(_abi.FP32C, used.lanes_per_column, used.block_threads,
+                                 used.columns_per_tile, 0, 0) if head == _abi.FP32C
+                    else _abi.RunOpts(head, 0, 0, 0, 0, 0))
         for i in range(reps + 1):   # the first pass warms up
             torch.cuda.synchronize()
             t0 = time.perf_counter()
@@ -680,23 +799,56 @@ def ours(args, rank, world, local):
     e2e_value = world * n_pts / float(np.mean(e2e_times))
 
     if rank == 0:
-        fp64 = None if args.no_fp64 else fp64_compare(scans, descs, value / world, dev)
+        # accuracy against FP64 (the oracle's arithmetic; bit-identical to the
+        # reference on LJ/Coulomb terms)
+        fp64 = None
+        if not args.no_fp64:
+            head_pts = host_points(outs)
+            fast_pts = host_points(outs32) if outs32 is not None else None
+            refs, npts64, ms64, subset = fp64_reference(scans, descs, dev)
+            rate64 = npts64 / (ms64 / 1000.0)
+            if rigid:
+                # the crop's own relaxations in both precisions
+                cmp_head = np.concatenate([s.run(head)[0] for s, _, _ in refs])
+                cmp_fast = None
+            else:
+                cmp_head = np.concatenate([pick(h, cols, nz) for h, (_, cols, _) in zip(head_pts, refs)])
+                cmp_fast = (np.concatenate([pick(h, cols, nz) for h, (_, cols, _) in zip(fast_pts, refs)])
+                            if fast_pts is not None else None)
+            p64 = np.concatenate([p for _, _, p in refs])
+            fp64 = {"points_per_s": rate64, "points": npts64, "subset": subset, "kernel_ms": ms64,
+                    "speedup_vs_fp64": {head_name: value / world / rate64},
+                    head_name: err_stats(cmp_head, p64)}
+            if cmp_fast is not None:
+                fp64["FP32C"] = err_stats(cmp_fast, p64)
+                fp64["speedup_vs_fp64"]["FP32C"] = fast["points_per_s"] / world / rate64
+            if rigid:
+                for s, _, _ in refs:
+                    s.close()
         peak_tflops = fp32_peak(dev)
-        # flops of the relax kernel: per-scan flops per pair term, weighted by
-        # each scan's share of the pair terms (points x terms)
+        # algorithmic flops of the relax: per-scan flops per force evaluation,
+        # weighted by each scan's share of the pair terms (points x terms)
         wts = np.array([d.n_points * max(d.c.n_atoms, 1) for d in descs], dtype=float)
         fpe = np.array([term_flops(d) for d in descs], dtype=float)
+        ms_relax = ms_part["relax"]
         relax_flops = st.force_evals * float((wts * fpe).sum() / wts.sum()) if fpe.any() else 0.0
-        relax_line = None
+        kname = "relaxdf_kernel + repair64_kernel" if head == _abi.DF else "relax32_kernel"
         if fpe.any():
             relax_line = fp32_roofline(relax_flops / (ms_relax / 1000.0) / 1e12, peak_tflops, {
-                "traffic": DRAM_BYTES_PER_POINT * n_pts,
-                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one "
-                                  "285x285x41 cluster launch, scaled by points (the output "
-                                  "records are the traffic)",
-                "kernel": "relax32_kernel", "kernel_ms": ms_relax,
+                "traffic": POINT_BYTES * n_pts,
+                "traffic_source": "algorithmic output bytes (64 B per point, written once); the "
+                                  "ncu captures in profiles/ measure the DRAM bytes per point",
+                "kernel": kname, "kernel_ms": ms_relax,
+                "kernel_ms_source": ("events recorded inside the timed graph replays"
+                                     if step.external else
+                                     "events around the same launches (no external graph events)"),
                 "flops_per_force_eval": float((wts * fpe).sum() / wts.sum()),
                 "force_evals": int(st.force_evals)})
+            if head == _abi.DF:
+                relax_line["note"] = ("double-float arithmetic: every algorithmic FP64 flop costs "
+                                      "about 10-25 FP32-pipe instructions, so the fraction of the "
+                                      "FP32 peak is low by design; MAFM_FP32C (fast_path) is the "
+                                      "FP32-arithmetic kernel")
         else:
             hp, src = hbm_peak()
             gbs = st.force_evals * BYTES_LOOKUP / (ms_relax / 1000.0) / 1e9
@@ -711,6 +863,7 @@ def ours(args, rank, world, local):
                                   "L2 hit 83 % at 3 % L2 throughput, DRAM 20 GB/s, issue 43 %"}
         rooflines = [(ms_relax, relax_line)]
         if rigid:
+            ms_build = ms_part["grid_build"]
             nodes = sum(rigid_nodes(s.desc.c) for s in rigid)
             gflops = sum(rigid_nodes(s.desc.c) * term_flops(s.desc, direct=True) for s in rigid)
             rooflines.append((ms_build, fp32_roofline(gflops / (ms_build / 1000.0) / 1e12,
@@ -718,47 +871,66 @@ def ours(args, rank, world, local):
                 "kernel": "grid_build32_kernel", "kernel_ms": ms_build, "nodes": nodes,
                 "flops_per_node": float(gflops / nodes)})))
         if adjoint:
-            rooflines.append((ms_adj, {"kernel": "adjoint32_kernel (FP32C)", "kernel_ms": ms_adj,
-                                       "bound": "fp32", "note": "FP32 per-term Jacobians and "
-                                       "parameter derivatives, FP64 3x3 solve per point"}))
+            rooflines.append((ms_part["adjoint"], {"kernel": "adjoint32_kernel (FP32C)",
+                                                   "kernel_ms": ms_part["adjoint"], "bound": "fp32",
+                                                   "note": "FP32 per-term Jacobians and parameter "
+                                                           "derivatives, FP64 3x3 solve per point"}))
+        if fast is not None:
+            f32 = fast["force_evals"] * float((wts * fpe).sum() / wts.sum())
+            rooflines.append((fast["ms_per_step"], fp32_roofline(
+                f32 / (fast["ms_per_step"] / 1000.0) / 1e12, peak_tflops,
+                {"kernel": "relax32_kernel (MAFM_FP32C, the fast path)",
+                 "kernel_ms": fast["ms_per_step"]})))
         rooflines.sort(key=lambda r: -r[0])
+        main_line = relax_line if not rigid else rooflines[0][1]
         threads = cpu_threads()
         if args.cpu_seconds > 0:
-            cpu_value, cpu_sample = cpu_rate("adjoint" if adjoint else "forward", descs, threads,
-                                             args.cpu_seconds)
-            cpu = {"value": cpu_value, "unit": UNIT, "cores": threads, "kind": "port",
+            cpu_value, cpu_sample, cpu_kind, _, _ = cpu_rate("adjoint" if adjoint else "forward",
+                                                             inputs, descs, threads,
+                                                             args.cpu_seconds, tmp)
+            cpu = {"value": cpu_value, "unit": UNIT, "cores": threads, "kind": cpu_kind,
                    "sample": cpu_sample}
         else:
             cpu = None
-        launches = args.steps * (1 + len(rigid) + (1 if adjoint else 0))
+        launches = args.steps * ((2 if head == _abi.DF else 1) + len(rigid) + (1 if adjoint else 0))
         step_text = ("rigid grid rebuild + relax" if rigid else
                      "relax + adjoint" if adjoint else "relax")
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f32 (compensated sums, double-float positions and energy)",
+            "dtype": ("f32 double-float (pairs of FP32 numbers, 48-bit significand) on the FP32 "
+                      "pipes; near-tie columns in f64" if head == _abi.DF else
+                      "f32 (compensated sums, double-float positions and energy)"),
             "data": "synthetic",
             "config": {"workload": desc_text, "scans": n, "points_per_step": n_pts,
-                       "precision": "FP32C", "step": step_text,
-                       "launch": {"lanes_per_column": used.lanes_per_column,
-                                  "block_threads": used.block_threads,
-                                  "columns_per_tile": used.columns_per_tile,
-                                  "chosen_by": ("autotuner" if tune_ms is not None else
-                                                "forced" if (args.lanes or args.block or args.tile)
-                                                else "default"),
-                                  "column_order": ("natural (rigid grid: no pair terms to cost)"
-                                                   if rigid else "expected cost, descending"),
-                                  "cuda_graph": True},
+                       "precision": head_name, "step": step_text,
+                       "launch": ({"kernel": "relaxdf_kernel: persistent, one column per lane, a lane "
+                                             "takes the next column from the queue as soon as its "
+                                             "own ends (columns in expected-cost order); "
+                                             "repair64_kernel: one warp per listed column",
+                                   "cuda_graph": True}
+                                  if head == _abi.DF else
+                                  {"lanes_per_column": used.lanes_per_column,
+                                   "block_threads": used.block_threads,
+                                   "columns_per_tile": used.columns_per_tile,
+                                   "chosen_by": ("autotuner" if tune_ms is not None else
+                                                 "forced" if (args.lanes or args.block or args.tile)
+                                                 else "default"),
+                                   "column_order": ("natural (rigid grid: no pair terms to cost)"
+                                                    if rigid else "expected cost, descending"),
+                                   "cuda_graph": True}),
                        "l2": f"{L2_FLUSH_BYTES >> 20} MiB buffer written between timed steps",
                        "fire_steps_per_step": int(st.total_steps),
                        "pair_terms_per_step": int(st.pair_evals),
+                       "fp64_columns_per_step": int(st.fp64_columns),
                        "scan_create_s": t_create, "first_grid_build_s": t_grid,
                        "parallelism": f"replica per GPU x{world}"},
             "pair_terms_per_s": st.pair_evals * world / (ms / 1000.0),
-            "roofline": rooflines[0][1],
-            "roofline_other": [r[1] for r in rooflines[1:]],
+            "roofline": main_line,
+            "roofline_other": [r[1] for r in rooflines if r[1] is not main_line],
             "fp64_gpu": fp64,
+            "fast_path": fast,
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h)},
@@ -769,7 +941,7 @@ def ours(args, rank, world, local):
             line["adjoint"] = {"loss_grad_norms": {"dpos": float(np.linalg.norm(dpos)),
                                                    "dcharge": float(np.linalg.norm(dq)),
                                                    "dpair": float(np.linalg.norm(dpair))},
-                               "forward_ms": ms_relax, "adjoint_ms": ms_adj}
+                               "forward_ms": ms_relax, "adjoint_ms": ms_part["adjoint"]}
         print(json.dumps(line))
     L.mafm_plan_destroy(plan)
     if world > 1:

@@ -82,8 +82,8 @@ def build(verbose: bool = False) -> str:
     cli_src = os.path.join(CSRC, "mechafm_gpu.cpp")
     if os.path.exists(cli_src):
         os.makedirs(BIN_DIR, exist_ok=True)
-        _run(["g++", "-O2", "-std=c++17", "-Wall", "-ffp-contract=off", "-I" + INCLUDE, cli_src,
-              "-o", CLI, "-L" + HERE, "-lmafm", "-Wl,-rpath,$ORIGIN/.."])
+        _run(["g++", "-O2", "-std=c++17", "-Wall", "-ffp-contract=off", "-pthread", "-I" + INCLUDE,
+              cli_src, "-o", CLI, "-L" + HERE, "-lmafm", "-Wl,-rpath,$ORIGIN/.."])
     return LIB
 
 

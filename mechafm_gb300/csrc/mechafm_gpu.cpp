@@ -3,16 +3,27 @@
 //
 // Same arguments, input/xyz/parameter/cube files, stdout banners and option
 // echo, error messages and exit status, scan-%06.3f.dat[.gz] files and
-// statistics.txt.  The relaxation runs through libmafm's C ABI.  By default it
-// runs the FP64 kernel, whose results are those of the reference; setting
-// MAFM_PRECISION=fp32c selects the FP32-compensated kernel.  A flexible
-// molecule runs the FP64 flexible kernel and writes the middle pixel's
-// state_*.xyz files like the reference.  MAFM_DEVICE picks the GPU (default 0).
+// statistics.txt.  The relaxation runs through libmafm's C ABI.  By default a
+// scan over pair terms (and the external field) runs the double-float kernel,
+// whose points take the reference's FP64 steps and agree with its positions
+// and forces to about 1e-10, and a rigid-grid scan the FP64 kernel;
+// MAFM_PRECISION=fp64 / df / fp32c selects the plain FP64 kernel (the
+// reference's bits), the double-float kernel or the faster FP32-compensated
+// kernel.  A flexible molecule runs the FP64 flexible kernel and writes the
+// middle pixel's state_*.xyz files like the reference.  MAFM_DEVICE picks the
+// GPU (default 0).
+//
+// The scan runs in ten chunks of pixel rows (the reference's ten progress
+// lines).  While the GPU relaxes a chunk, this thread formats and writes the
+// previous one (mafm_writer_append; gzip runs in its own processes), so the
+// text output, which takes longer than the relaxation at GPU speed, overlaps
+// it; the files are byte-identical to writing every point at the end.
 #include <chrono>
 #include <cstdarg>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <future>
 #include <string>
 #include <vector>
 
@@ -60,7 +71,6 @@ int main(int argc, char* argv[]) {
         if (system(cmd.c_str()) != 0) error(("cannot create " + outdir).c_str());
     }
     const char* prec_env = getenv("MAFM_PRECISION");
-    const int precision = (prec_env && !strcmp(prec_env, "fp32c")) ? MAFM_FP32C : MAFM_FP64;
     const char* dev_env = getenv("MAFM_DEVICE");
     const int device = dev_env ? atoi(dev_env) : 0;
 
@@ -70,6 +80,10 @@ int main(int argc, char* argv[]) {
     check(mafm_input_desc(in, &d));
     int32_t gzip = 0, statistics = 0, bufsize = 0;
     check(mafm_input_output_opts(in, &gzip, &statistics, &bufsize));
+    int precision = d.rigidgrid ? MAFM_FP64 : MAFM_DF;
+    if (prec_env && !strcmp(prec_env, "fp64")) precision = MAFM_FP64;
+    if (prec_env && !strcmp(prec_env, "fp32c")) precision = MAFM_FP32C;
+    if (prec_env && !strcmp(prec_env, "df") && !d.rigidgrid) precision = MAFM_DF;
 
     // openUniverse (mechafm.cpp:37-80)
     const int n_total = d.nx * d.ny * d.nz;
@@ -113,33 +127,55 @@ int main(int argc, char* argv[]) {
             next_report += report_interval;
         }
     };
-    std::vector<mafm_point> pts((size_t)n_total);
     uint64_t total_steps = 0;
     const int chunks = 10;
     // flexible molecules: the middle pixel's states (simulation.cpp:114-116)
     const int state_col = (d.nx * d.ny) / 2;
-    std::vector<double> states(d.flexible ? (size_t)d.nz * (d.n_atoms + 2) * 3 : 0);
-    for (int c = 0; c < chunks; ++c) {
+    struct Chunk {
+        int cb = 0, ce = 0;
+        std::vector<mafm_point> pts;
+        std::vector<double> states;
+        bool with_states = false;
+        uint64_t steps = 0;
+    };
+    // relax chunk c into ch (on a worker thread; only the GPU and ch are touched)
+    auto relax = [&](int c, Chunk* ch) {
         const int i0 = (int)((long long)d.nx * c / chunks), i1 = (int)((long long)d.nx * (c + 1) / chunks);
-        if (i1 <= i0) continue;
-        const int cb = i0 * d.ny, ce = i1 * d.ny;
+        ch->cb = i0 * d.ny;
+        ch->ce = i1 * d.ny;
+        ch->pts.resize((size_t)(ch->ce - ch->cb) * d.nz);
         mafm_run_stats st{};
-        if (flex) {
-            const bool with_states = state_col >= cb && state_col < ce;
-            check(mafm_flex_run(flex, cb, ce, pts.data() + (size_t)cb * d.nz, &st, state_col,
-                                with_states ? states.data() : nullptr, nullptr));
-            if (with_states) check(mafm_write_states(in, states.data(), state_col, outdir.c_str()));
-        } else {
-            mafm_run_opts o{};
-            o.precision = precision;
-            o.col_begin = cb;
-            o.col_end = ce;
-            check(mafm_run(scan, &o, pts.data() + (size_t)cb * d.nz, &st, nullptr));
+        if (ch->ce > ch->cb) {
+            if (flex) {
+                ch->with_states = state_col >= ch->cb && state_col < ch->ce;
+                if (ch->with_states) ch->states.resize((size_t)d.nz * (d.n_atoms + 2) * 3);
+                check(mafm_flex_run(flex, ch->cb, ch->ce, ch->pts.data(), &st, state_col,
+                                    ch->with_states ? ch->states.data() : nullptr, nullptr));
+            } else {
+                mafm_run_opts o{};
+                o.precision = precision;
+                o.col_begin = ch->cb;
+                o.col_end = ch->ce;
+                check(mafm_run(scan, &o, ch->pts.data(), &st, nullptr));
+            }
         }
-        total_steps += st.total_steps;
-        report(ce);
+        ch->steps = st.total_steps;
+    };
+    mafm_writer* writer = nullptr;
+    check(mafm_writer_open(in, outdir.c_str(), gzip, &writer));
+    Chunk buf[2];
+    std::future<void> pending = std::async(std::launch::async, relax, 0, &buf[0]);
+    for (int c = 0; c < chunks; ++c) {
+        pending.get();
+        Chunk& ch = buf[c % 2];
+        if (c + 1 < chunks) pending = std::async(std::launch::async, relax, c + 1, &buf[(c + 1) % 2]);
+        if (ch.ce <= ch.cb) continue;
+        if (ch.with_states) check(mafm_write_states(in, ch.states.data(), state_col, outdir.c_str()));
+        total_steps += ch.steps;
+        report(ch.ce);
+        check(mafm_writer_append(writer, ch.pts.data(), ch.cb, ch.ce));
     }
-    check(mafm_write_output(in, pts.data(), outdir.c_str(), gzip));
+    check(mafm_writer_close(writer));
     if (scan) check(mafm_scan_destroy(scan));
     if (flex) check(mafm_flex_destroy(flex));
 

@@ -14,7 +14,11 @@ tests/golden/slab_c3/ref.npz holds
                      scan's heights, and the reference's external-field force
                      and energy there: ElectrostaticPotentialInteraction
                      (interactions.cpp:53-242), whose field the reference
-                     computes with kiss_fft (fft.cpp:11-94, kiss_fftnd.c)
+                     computes with kiss_fft (fft.cpp:11-94, kiss_fftnd.c).
+                     Sampled on the same slab with rigidgrid off (field_spec):
+                     with a rigid grid the reference folds the interaction
+                     into the grid, and its tip–surface list holds no
+                     ElectrostaticPotentialInteraction to evaluate
   steps, tip, force, energy
                      the reference's relaxed points of the 8 x 8 pixel block
                      at the origin of the same scan geometry (rigid grid of
@@ -48,6 +52,11 @@ def spec():
     return synth.slab(**SPEC)
 
 
+def field_spec():
+    """The same slab and cube without the rigid grid (the field samples)."""
+    return synth.slab(**SPEC, rigidgrid=False)
+
+
 def file_hashes(folder: str) -> dict:
     out = {}
     for fn in sorted(os.listdir(folder)):
@@ -75,17 +84,22 @@ def main():
     os.makedirs(FOLDER)
     work = os.path.join(FOLDER, "_work")
     inp = spec().write(work)
+    fwork = os.path.join(FOLDER, "_field")
+    finp = field_spec().write(fwork)
     pts = sample_points()
-    fe = oracle.ref_sample(inp, pts, "sample_es", os.path.join(work, "_s"))
+    fe = oracle.ref_sample(finp, pts, "sample_es", os.path.join(fwork, "_s"))
+    if not np.abs(fe).max() > 0:
+        raise SystemExit("the reference sampled no external field")
     rec = oracle.ref_scan(inp, os.path.join(work, "_ref.bin"), (0, 8), (0, 8))
     meta = {"spec": SPEC, "input": os.path.basename(inp), "sha256": file_hashes(work),
-            "points": int(len(rec))}
+            "sha256_field": file_hashes(fwork), "points": int(len(rec))}
     np.savez_compressed(os.path.join(FOLDER, "ref.npz"), es_pts=pts, es_fe=fe,
                         steps=rec[:, 3].astype(np.int32), tip=rec[:, 4:7], force=rec[:, 13:16],
                         energy=rec[:, 16])
     with open(os.path.join(FOLDER, "meta.json"), "w") as f:
         json.dump(meta, f, indent=1, sort_keys=True)
     shutil.rmtree(work)
+    shutil.rmtree(fwork)
     print("slab_c3:", N_SAMPLES, "field samples,", len(rec), "points, mean steps",
           rec[:, 3].mean())
 

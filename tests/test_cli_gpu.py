@@ -1,8 +1,9 @@
 """The drop-in executable `mechafm-gpu INPUT OUTPUT` on the GPU against the
 reference executable's own output (tests/golden/cli_*): every scan-file row,
-and for a flexible molecule the middle pixel's state_*.xyz files.  The FP64
-kernels match the reference to rounding (bit for bit on LJ terms), so the
-printed numbers are compared to within one unit of their last printed digit.
+and for a flexible molecule the middle pixel's state_*.xyz files.  The
+default (double-float) and the plain FP64 kernels match the reference to
+rounding (FP64 bit for bit on LJ terms), so the printed numbers are compared
+to within one unit of their last printed digit.
 """
 import os
 import subprocess
@@ -27,19 +28,25 @@ def _rows(path):
     return out
 
 
-def _run(name, tmp_path):
+def _run(name, tmp_path, precision=""):
     folder = os.path.join(GOLDEN, name)
     inp = os.path.join(folder, MANIFEST[name]["input"])
     out = str(tmp_path / "out") + "/"
-    r = subprocess.run([CLI, inp, out], cwd=folder, capture_output=True, text=True, timeout=600)
+    env = dict(os.environ)
+    env.pop("MAFM_PRECISION", None)
+    if precision:
+        env["MAFM_PRECISION"] = precision
+    r = subprocess.run([CLI, inp, out], cwd=folder, capture_output=True, text=True, timeout=600,
+                       env=env)
     assert r.returncode == 0, r.stderr[-2000:]
     return folder, out, r.stdout
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("precision", ["", "fp64"])
 @pytest.mark.parametrize("name", CASES)
-def test_cli_rows_match_reference_executable(name, tmp_path):
-    folder, out, stdout = _run(name, tmp_path)
+def test_cli_rows_match_reference_executable(name, precision, tmp_path):
+    folder, out, stdout = _run(name, tmp_path, precision)
     got_lines = []
     for fn in sorted(os.listdir(out)):
         if fn.startswith("scan-"):

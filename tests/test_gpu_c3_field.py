@@ -3,7 +3,9 @@
 The 2048-atom periodic slab with its 160 x 160 x 120 Hartree cube (the
 bench's slab workload; radices 2^5 5 and 2^3 3 5, which take cuFFT down
 other paths than the 24-voxel fixtures): the seeded generator writes the
-input files again, their SHA-256 must equal the fixture's, then
+input files again (the rigid-grid scan, and the same slab without the grid,
+on which the reference's field was sampled: with a rigid grid the reference
+folds the field into the grid), their SHA-256 must equal the fixture's, then
 
   * the FP64 field (cuFFT Z2Z) at 4000 seeded tip positions over the cell
     equals the reference's (kiss_fft, ElectrostaticPotentialInteraction,
@@ -41,17 +43,25 @@ def c3(tmp_path_factory):
     work = str(tmp_path_factory.mktemp("c3"))
     inp = g.spec().write(work)
     assert g.file_hashes(work) == meta["sha256"], "regenerated inputs differ from the fixture's"
+    fwork = str(tmp_path_factory.mktemp("c3_field"))
+    finp = g.field_spec().write(fwork)
+    assert g.file_hashes(fwork) == meta["sha256_field"], "regenerated inputs differ from the fixture's"
     ref = dict(np.load(os.path.join(FOLDER, "ref.npz")))
-    desc = Input(inp).desc()
-    scan = Scan(desc, device=0)
-    yield scan, ref
+    scan = Scan(Input(inp).desc(), device=0)
+    field = Scan(Input(finp).desc(), device=0)
+    yield scan, field, ref
     scan.close()
+    field.close()
 
 
 @pytest.mark.parametrize("precision,tol", [(_abi.FP64, 1e-9), (_abi.FP32C, 1e-4)])
 def test_field_samples_match_kiss_fft(c3, precision, tol):
-    scan, ref = c3
-    fe = scan.sample(ref["es_pts"], precision=precision, what=1)
+    """Sampled like the reference's samples: on the slab without the rigid
+    grid; the rigid-grid scan's own field (what the grid build samples) must
+    give the same values."""
+    scan, field, ref = c3
+    fe = field.sample(ref["es_pts"], precision=precision, what=1)
+    np.testing.assert_array_equal(scan.sample(ref["es_pts"], precision=precision, what=1), fe)
     want = ref["es_fe"]
     scale = np.maximum(np.abs(want), 1e-2)
     err = np.abs(fe - want) / scale
@@ -59,7 +69,7 @@ def test_field_samples_match_kiss_fft(c3, precision, tol):
 
 
 def test_block_fp64_matches_reference(c3):
-    scan, ref = c3
+    scan, _, ref = c3
     pts, _ = scan.run(_abi.FP64)
     same = pts["steps"] == ref["steps"]
     assert same.mean() >= 0.99, same.mean()
@@ -68,7 +78,7 @@ def test_block_fp64_matches_reference(c3):
 
 
 def test_block_fp32c_within_bar(c3):
-    scan, ref = c3
+    scan, _, ref = c3
     pts, _ = scan.run(_abi.FP32C)
     tip = np.abs(pts["tip"] - ref["tip"]).max(axis=1)
     fz = np.abs(pts["force"][:, 2] - ref["force"][:, 2]) / np.maximum(np.abs(ref["force"][:, 2]), 0.01)
