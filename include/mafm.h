@@ -69,7 +69,11 @@ enum {
                         numbers (48-bit significand) on the FP32 pipes, so FIRE
                         takes FP64's decisions; a column in which a decision
                         still came within the double-float error margin of its
-                        threshold is re-relaxed in FP64 (MAFM_PT_FP64) */
+                        threshold is re-relaxed in FP64 (MAFM_PT_FP64).  A
+                        rigid grid is built in double-float too; the FP64
+                        re-relaxation reads its FP64 copy (the grid's nodes
+                        then agree with an FP64 build to about 1e-14, not bit
+                        for bit) */
 };
 
 /* Per-point status bits (mafm_point.status). */
@@ -164,7 +168,9 @@ typedef struct mafm_point {
 typedef struct mafm_run_opts {
     int32_t precision;          /* MAFM_FP64 or MAFM_FP32C */
     int32_t lanes_per_column;   /* FP32C: 1,2,4,8,16,32 lanes share a column; 0 = default
-                                   (from the column count; mafm_autotune measures) */
+                                   (from the column count; mafm_autotune measures).
+                                   MAFM_DF: 1,2,4,8 lanes share a column's terms; 0 =
+                                   default */
     int32_t block_threads;      /* 0 = default (256) */
     int32_t columns_per_tile;   /* FP32C: columns a warp takes from the shared queue at a
                                    time; 0 = default (1 for a large single scan, else one
@@ -407,8 +413,9 @@ int mafm_scan_grid_copy(const mafm_scan* scan, int32_t what, double* out);
  * stream: Simulation::buildTipGridInteractions (simulation.cpp:420-501), which
  * the reference runs once per scan before the pixel loop.  mafm_run builds the
  * grid on first use; this call rebuilds it on demand.  The first call for a
- * precision allocates the grid; later calls only launch the build kernel, so
- * they may be captured in a CUDA graph together with mafm_plan_launch.
+ * precision allocates the grid; later calls only launch the build kernel(s)
+ * (MAFM_DF: the double-float build and its FP64 copy), so they may be
+ * captured in a CUDA graph together with mafm_plan_launch.
  * No-op (MAFM_OK) for a scan without a rigid grid. */
 int mafm_scan_build_grid(mafm_scan* scan, int32_t precision, void* stream);
 

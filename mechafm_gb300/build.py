@@ -4,7 +4,10 @@ nvcc compiles each CUDA translation unit for sm_103a only; g++ compiles the
 host front-end.  Host code everywhere is compiled with -ffp-contract=off so
 that it computes the same bits as the reference's x86-64 build (no fused
 multiply-add in the host arithmetic of centring, mixing and matrix inverses).
-relax64.cu is compiled with -fmad=false for the same reason on the device.
+relax64.cu is compiled with -fmad=false for the same reason on the device,
+and so is relaxdf.cu, whose FP64 re-relaxation of near-tie columns must give
+relax64.cu's bits (its double-float arithmetic uses explicitly rounded
+intrinsics, which -fmad does not touch).
 """
 from __future__ import annotations
 
@@ -51,7 +54,7 @@ def _units():
     return [
         ([nv] + common + ["-fmad=false", os.path.join(CSRC, "relax64.cu")], "relax64.o"),
         ([nv] + common + [os.path.join(CSRC, "relax32.cu")], "relax32.o"),
-        ([nv] + common + [os.path.join(CSRC, "relaxdf.cu")], "relaxdf.o"),
+        ([nv] + common + ["-fmad=false", os.path.join(CSRC, "relaxdf.cu")], "relaxdf.o"),
         ([nv] + common + [os.path.join(CSRC, "scan.cu")], "scan.o"),
         ([nv] + common + [os.path.join(CSRC, "noalloc.cu")], "noalloc.o"),
         ([nv] + common + [os.path.join(CSRC, "adjoint.cu")], "adjoint.o"),

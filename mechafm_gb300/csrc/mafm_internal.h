@@ -70,7 +70,8 @@ inline unsigned long long watchdog_ns_from_env() {
 enum : uint32_t {
     ERR_GRID_INDEX = 1u << 16,   // corner outside a non-periodic grid (force_grid.cpp:236-240)
     ERR_STAGE_TIMEOUT = 1u << 17, // bounded wait on the atom staging barrier expired
-    ERR_WATCHDOG = 1u << 18       // a persistent warp ran past its time limit
+    ERR_WATCHDOG = 1u << 18,      // a persistent warp ran past its time limit
+    ERR_REPAIR_WAIT = 1u << 19    // a bounded wait for a near-tie column's list entry expired
 };
 
 struct __align__(16) AtomRec64 {

@@ -3,13 +3,12 @@
 //
 // Same arguments, input/xyz/parameter/cube files, stdout banners and option
 // echo, error messages and exit status, scan-%06.3f.dat[.gz] files and
-// statistics.txt.  The relaxation runs through libmafm's C ABI.  By default a
-// scan over pair terms (and the external field) runs the double-float kernel,
-// whose points take the reference's FP64 steps and agree with its positions
-// and forces to about 1e-10, and a rigid-grid scan the FP64 kernel;
-// MAFM_PRECISION=fp64 / df / fp32c selects the plain FP64 kernel (the
-// reference's bits), the double-float kernel or the faster FP32-compensated
-// kernel.  A flexible molecule runs the FP64 flexible kernel and writes the
+// statistics.txt.  The relaxation runs through libmafm's C ABI.  By default
+// it runs the double-float kernel, whose points take the reference's FP64
+// steps and agree with its positions and forces to about 1e-10 (a rigid grid
+// is built in double-float too); MAFM_PRECISION=fp64 / df / fp32c selects the
+// plain FP64 kernel (the reference's bits), the double-float kernel or the
+// faster FP32-compensated kernel.  A flexible molecule runs the FP64 flexible kernel and writes the
 // middle pixel's state_*.xyz files like the reference.  MAFM_DEVICE picks the
 // GPU (default 0).
 //
@@ -80,10 +79,9 @@ int main(int argc, char* argv[]) {
     check(mafm_input_desc(in, &d));
     int32_t gzip = 0, statistics = 0, bufsize = 0;
     check(mafm_input_output_opts(in, &gzip, &statistics, &bufsize));
-    int precision = d.rigidgrid ? MAFM_FP64 : MAFM_DF;
+    int precision = MAFM_DF;
     if (prec_env && !strcmp(prec_env, "fp64")) precision = MAFM_FP64;
     if (prec_env && !strcmp(prec_env, "fp32c")) precision = MAFM_FP32C;
-    if (prec_env && !strcmp(prec_env, "df") && !d.rigidgrid) precision = MAFM_DF;
 
     // openUniverse (mechafm.cpp:37-80)
     const int n_total = d.nx * d.ny * d.nz;

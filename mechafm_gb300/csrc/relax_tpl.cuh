@@ -221,9 +221,11 @@ __device__ void relax_column_t(Ev& ev, const P& p, long long c, mafm_point* o, b
         status_or |= (unsigned)st;
         if (writer) {
             if (replace) {
-                const mafm_point old = o[k];
-                steps -= old.steps;
-                st |= (old.status & MAFM_PT_NEAR_TIE) | MAFM_PT_FP64;
+                // through L2: the record may have been written on another SM
+                // (the double-float kernel's placeholders) just before
+                const int old_steps = __ldcg(&o[k].steps), old_status = __ldcg(&o[k].status);
+                steps -= old_steps;
+                st |= (old_status & MAFM_PT_NEAR_TIE) | MAFM_PT_FP64;
             }
             mafm_point r;
             r.tip[0] = t_double(s.tip.x); r.tip[1] = t_double(s.tip.y); r.tip[2] = t_double(s.tip.z);

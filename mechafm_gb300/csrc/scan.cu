@@ -220,8 +220,12 @@ struct mafm_scan {
     mafm::DevBuf<mafm::BatchScan> batch;
     mafm::DevBuf<mafm_point> stage;
     mafm::DevBuf<int> order;             // columns by descending expected cost
-    mafm::DevBuf<mafm::AtomRecDF> atomsdf;     // terms in double-float (MAFM_DF)
+    mafm::DevBuf<mafm::TermPairDF> pairsdf;    // terms in double-float pairs (MAFM_DF)
+    int df_lj_pairs = 0, df_morse_pairs = 0;
     mafm::DevBuf<mafm::NodeDF> esdf;           // external field in double-float
+    mafm::DevBuf<mafm::NodeDF> griddf;         // rigid grid built in double-float
+    mafm::DevBuf<mafm::Node64> griddf64;       //   and its FP64 copy (re-relaxation)
+    bool griddf_built = false;
     mafm::DevBuf<mafm::BatchDF> batchdf;       // descriptor of a double-float run
     mafm::DevBuf<unsigned long long> repair;   // columns to re-relax in FP64
     bool order_built = false;
@@ -379,13 +383,11 @@ void pack_terms(mafm_scan& s, const mafm_scan_desc& d) {
         cuda_check(cudaMemcpy(s.atoms32.p, t32.data(), t32.size() * sizeof(AtomRec32),
                               cudaMemcpyHostToDevice), "upload terms");
     }
-    // double-float copy for MAFM_DF
-    std::vector<AtomRecDF> tdf;
-    tdf.reserve(t64.size());
-    for (const AtomRec64& r : t64) tdf.push_back(term_df(r));
-    s.atomsdf.alloc(std::max<size_t>(tdf.size(), 1));
+    // double-float pairs for MAFM_DF
+    const std::vector<TermPairDF> tdf = term_pairs_df(t64, s.df_lj_pairs, s.df_morse_pairs);
+    s.pairsdf.alloc(std::max<size_t>(tdf.size(), 1));
     if (!tdf.empty())
-        cuda_check(cudaMemcpy(s.atomsdf.p, tdf.data(), tdf.size() * sizeof(AtomRecDF),
+        cuda_check(cudaMemcpy(s.pairsdf.p, tdf.data(), tdf.size() * sizeof(TermPairDF),
                               cudaMemcpyHostToDevice), "upload terms");
     s.P.n_terms = (int)t64.size();
     s.P.n_terms_direct = d.rigidgrid ? 0 : s.P.n_terms;
@@ -538,6 +540,14 @@ ScanParams build_params(const mafm_scan& s) {
     return p;
 }
 
+// The FP64 descriptor that a double-float launch's re-relaxation reads: over
+// a rigid grid, the FP64 copy of the double-float grid.
+ScanParams build_params_for(const mafm_scan& s, bool df) {
+    ScanParams p = build_params(s);
+    if (df && s.d.rigidgrid) p.grid.g64 = s.griddf64.p;
+    return p;
+}
+
 // Parameters of the grid build: every tip–surface term plus the external field.
 ScanParams build_grid_params(const mafm_scan& s) {
     ScanParams p = s.P;
@@ -573,6 +583,29 @@ void ensure_grid(mafm_scan& s, bool fp64, cudaStream_t st, bool rebuild = false)
         s.grid32_built = true;
     }
     s.P.grid = s.grid_view;
+}
+
+// The double-float rigid grid (MAFM_DF) and its FP64 copy, built on first use
+// (rebuild: again).
+void ensure_grid_df(mafm_scan& s, cudaStream_t st, bool rebuild = false) {
+    if (!s.d.rigidgrid) return;
+    if (rebuild) s.griddf_built = false;
+    if (s.griddf_built) return;
+    const long long N = (long long)s.grid_view.n[0] * s.grid_view.n[1] * s.grid_view.n[2];
+    if (!s.griddf.p) s.griddf.alloc((size_t)N);
+    if (!s.griddf64.p) s.griddf64.alloc((size_t)N);
+    zero_counters(s, st);
+    ScanParams bp = build_grid_params(s);
+    bp.grid = s.grid_view;
+    const ScanParamsDF q = params_df(bp, s.pairsdf.p, s.df_lj_pairs, s.df_morse_pairs, s.esdf.p, s.griddf.p);
+    cuda_check(launch_grid_builddf(q, s.griddf.p, s.griddf64.p, &s.ctr.p->error_word, st), "grid build");
+    s.griddf_built = true;
+}
+
+// The grid a relaxation in precision prec reads, built if needed.
+void ensure_grid_for(mafm_scan& s, int prec, cudaStream_t st, bool rebuild = false) {
+    if (prec == MAFM_DF) ensure_grid_df(s, st, rebuild);
+    else ensure_grid(s, prec == MAFM_FP64, st, rebuild);
 }
 
 // Cost-ordered schedule of a scan's columns, built once: proxy on the GPU,
@@ -643,23 +676,16 @@ void check_device_errors(const RunCounters& c) {
                             "unspecified (destroy and recreate it)");
     if (c.error_word & ERR_WATCHDOG)
         fail(MAFM_E_DEVICE, "the relax kernel stopped at its watchdog time limit");
-}
-
-// The double-float path relaxes pair terms and the external field; a rigid
-// grid would need a double-float grid build.
-void check_df_supported(const mafm_scan& s) {
-    if (s.d.rigidgrid)
-        fail(MAFM_E_UNSUPPORTED, "MAFM_DF relaxes over pair terms and the external field; a scan "
-                                 "with a rigid force grid runs in MAFM_FP64 or MAFM_FP32C");
+    if (c.error_word & ERR_REPAIR_WAIT)
+        fail(MAFM_E_DEVICE, "a bounded wait for a near-tie column's re-relaxation entry expired; "
+                            "that column holds no results");
 }
 
 // Descriptor of a double-float run over columns [cb, ce) of a scan.
 BatchDF batch_df_entry(const mafm_scan& s, mafm_point* out, int cb, int ce, bool whole,
                        long long col_first) {
     BatchDF b{};
-    ScanParams p = s.P;
-    p.n_terms_direct = p.n_terms;
-    b.p = params_df(p, s.atomsdf.p, s.esdf.p);
+    b.p = params_df(s.P, s.pairsdf.p, s.df_lj_pairs, s.df_morse_pairs, s.esdf.p, s.griddf.p);
     b.out = out;
     b.col_first = col_first;
     b.col_begin = cb;
@@ -809,7 +835,6 @@ int mafm_run(mafm_scan* scan, const mafm_run_opts* opts, mafm_point* out, mafm_r
         const int prec = opts ? opts->precision : MAFM_FP64;
         if (prec != MAFM_FP64 && prec != MAFM_FP32C && prec != MAFM_DF)
             fail(MAFM_E_INVALID, "precision %d", prec);
-        if (prec == MAFM_DF) check_df_supported(*scan);
         const size_t n_pts = (size_t)(ce - cb) * scan->d.nz;
         if (n_pts == 0) {
             if (stats) *stats = mafm_run_stats{};
@@ -825,7 +850,7 @@ int mafm_run(mafm_scan* scan, const mafm_run_opts* opts, mafm_point* out, mafm_r
             scan->stage.alloc(n_pts);
             dout = scan->stage.p;
         }
-        ensure_grid(*scan, prec == MAFM_FP64, st);
+        ensure_grid_for(*scan, prec, st);
         const bool whole = cb == 0 && ce == n_cols_all;
         if (prec == MAFM_DF && whole) ensure_order(*scan, st);
         zero_counters(*scan, st);
@@ -836,7 +861,7 @@ int mafm_run(mafm_scan* scan, const mafm_run_opts* opts, mafm_point* out, mafm_r
         } else if (prec == MAFM_DF) {
             // double-float relaxation, then FP64 for the columns it lists
             BatchScan b{};
-            b.p = build_params(*scan);
+            b.p = build_params_for(*scan, true);
             b.out = dout;
             b.col_begin = cb;
             b.col_end = ce;
@@ -848,8 +873,9 @@ int mafm_run(mafm_scan* scan, const mafm_run_opts* opts, mafm_point* out, mafm_r
             cuda_check(cudaGetLastError(), "descriptor upload");
             const unsigned cap = (unsigned)(ce - cb);
             scan->repair.alloc(cap);
-            cuda_check(launch_relaxdf(scan->batchdf.p, 1, ce - cb, scan->ctr.p, scan->repair.p, cap,
-                                      watchdog_ns_from_env(), st), "double-float relax launch");
+            cuda_check(launch_relaxdf(scan->batchdf.p, scan->batch.p, 1, ce - cb, scan->ctr.p, scan->repair.p, cap,
+                                      watchdog_ns_from_env(), opts ? opts->lanes_per_column : 0, st),
+                       "double-float relax launch");
             cuda_check(launch_repair64(scan->batch.p, scan->repair.p, cap, -1, true, false, scan->ctr.p, st),
                        "FP64 re-relaxation launch");
         } else {
@@ -924,8 +950,7 @@ int mafm_run_batch(mafm_scan* const* scans, int32_t n_scans, const mafm_run_opts
             total_pts += (size_t)cols * s->d.nz;
             max_cols = std::max(max_cols, cols);
             total_cols += cols;
-            if (dfp) check_df_supported(*s);
-            else ensure_grid(*s, false, st);
+            ensure_grid_for(*s, prec, st);
             ensure_order(*s, st);
             max_terms = std::max(max_terms, s->d.rigidgrid ? 0 : s->P.n_terms);
         }
@@ -942,7 +967,7 @@ int mafm_run_batch(mafm_scan* const* scans, int32_t n_scans, const mafm_run_opts
         for (int i = 0; i < n_scans; ++i) {
             mafm_scan* s = scans[i];
             BatchScan& b = bs[i];
-            b.p = build_params(*s);
+            b.p = build_params_for(*s, dfp);
             b.out = !host_out ? outs[i] : pinned[i] ? pinned[i] : s0->stage.p + offsets[i];
             b.tile_begin = tiles;
             b.col_begin = 0;
@@ -975,8 +1000,9 @@ int mafm_run_batch(mafm_scan* const* scans, int32_t n_scans, const mafm_run_opts
         zero_counters(*s0, st);
         cuda_check(cudaEventRecord(s0->ev0, st), "cudaEventRecord");
         if (dfp) {
-            cuda_check(launch_relaxdf(dbd.p, n_scans, total_cols, s0->ctr.p, rlist.p, (unsigned)total_cols,
-                                      watchdog_ns_from_env(), st), "double-float relax launch");
+            cuda_check(launch_relaxdf(dbd.p, dbs.p, n_scans, total_cols, s0->ctr.p, rlist.p, (unsigned)total_cols,
+                                      watchdog_ns_from_env(), opts ? opts->lanes_per_column : 0, st),
+                       "double-float relax launch");
             cuda_check(launch_repair64(dbs.p, rlist.p, (unsigned)total_cols, -1, true, false, s0->ctr.p, st),
                        "FP64 re-relaxation launch");
         } else {
@@ -1113,11 +1139,11 @@ int mafm_scan_grid_info(const mafm_scan* scan, int32_t what, int32_t n[3], doubl
 int mafm_scan_build_grid(mafm_scan* scan, int32_t precision, void* stream) {
     return guarded([&] {
         if (!scan) fail(MAFM_E_INVALID, "null scan");
-        if (precision != MAFM_FP64 && precision != MAFM_FP32C)
+        if (precision != MAFM_FP64 && precision != MAFM_FP32C && precision != MAFM_DF)
             fail(MAFM_E_INVALID, "unknown precision %d", precision);
         if (!scan->d.rigidgrid) return;
         cuda_check(cudaSetDevice(scan->device), "cudaSetDevice");
-        ensure_grid(*scan, precision == MAFM_FP64, (cudaStream_t)stream, true);
+        ensure_grid_for(*scan, precision, (cudaStream_t)stream, true);
     });
 }
 
@@ -1190,6 +1216,7 @@ struct mafm_plan {
     long long cols = 0;
     mafm::DevBuf<mafm::BatchDF> listdf;
     mafm::DevBuf<unsigned long long> repair;
+    int df_lanes = 1;                          // lanes per column of the DF kernel
     mafm::RunCounters* host_ctr = nullptr;
     ~mafm_plan() {
         if (host_ctr) cudaFreeHost(host_ctr);
@@ -1201,11 +1228,12 @@ namespace {
 
 // Descriptor list of a batch (tile numbering for the persistent kernel).
 std::vector<BatchScan> batch_entries(mafm_scan* const* scans, int n, mafm_point* const* outs,
-                                     const Relax32Config& cfg, long long& tiles) {
+                                     const Relax32Config& cfg, long long& tiles, bool df) {
     std::vector<BatchScan> bs((size_t)n);
     tiles = 0;
     for (int i = 0; i < n; ++i) {
         bs[i] = scan_batch_entry(scans[i], outs[i]);
+        bs[i].p = build_params_for(*scans[i], df);
         bs[i].tile_begin = tiles;
         tiles += ((long long)bs[i].col_end + cfg.cols_per_tile - 1) / cfg.cols_per_tile;
     }
@@ -1227,14 +1255,13 @@ void plan_build(mafm_plan& p, mafm_scan* const* scans, int n, const mafm_run_opt
         if (!scans[i] || !outs[i]) fail(MAFM_E_INVALID, "null scan or output %d", i);
         if (scans[i]->device != p.device) fail(MAFM_E_INVALID, "scans of one plan must share a device");
         if (!is_device_ptr(outs[i])) fail(MAFM_E_INVALID, "plan outputs must be device memory");
-        if (p.dfp) check_df_supported(*scans[i]);
-        else ensure_grid(*scans[i], false, st);
+        ensure_grid_for(*scans[i], prec, st);
         ensure_order(*scans[i], st);
         cols += (long long)scans[i]->d.nx * scans[i]->d.ny;
         max_terms = std::max(max_terms, scan_direct_terms(scans[i]));
     }
     p.cfg = default_config(cols, max_terms, opts, n);
-    std::vector<BatchScan> bs = batch_entries(scans, n, outs, p.cfg, p.tiles);
+    std::vector<BatchScan> bs = batch_entries(scans, n, outs, p.cfg, p.tiles, p.dfp);
     p.n_scans = n;
     p.cols = cols;
     p.list.alloc(bs.size());
@@ -1243,6 +1270,7 @@ void plan_build(mafm_plan& p, mafm_scan* const* scans, int n, const mafm_run_opt
                                cudaMemcpyHostToDevice, st), "upload plan");
     std::vector<BatchDF> bd;
     if (p.dfp) {
+        p.df_lanes = df_lanes_per_column(cols, opts ? opts->lanes_per_column : 0);
         long long first = 0;
         for (int i = 0; i < n; ++i) {
             bd.push_back(batch_df_entry(*scans[i], outs[i], 0, bs[i].col_end, true, first));
@@ -1260,8 +1288,9 @@ void plan_build(mafm_plan& p, mafm_scan* const* scans, int n, const mafm_run_opt
 void plan_launch(mafm_plan& p, cudaStream_t st) {
     cuda_check(cudaMemsetAsync(p.ctr.p, 0, sizeof(RunCounters), st), "reset counters");
     if (p.dfp) {
-        cuda_check(launch_relaxdf(p.listdf.p, p.n_scans, p.cols, p.ctr.p, p.repair.p,
-                                  (unsigned)p.cols, p.cfg.watchdog_ns, st), "double-float relax launch");
+        cuda_check(launch_relaxdf(p.listdf.p, p.list.p, p.n_scans, p.cols, p.ctr.p, p.repair.p,
+                                  (unsigned)p.cols, p.cfg.watchdog_ns, p.df_lanes, st),
+                   "double-float relax launch");
         cuda_check(launch_repair64(p.list.p, p.repair.p, (unsigned)p.cols, -1, true, false, p.ctr.p, st),
                    "FP64 re-relaxation launch");
     } else {
@@ -1328,9 +1357,9 @@ int mafm_plan_config(const mafm_plan* plan, mafm_run_opts* opts) {
         if (!plan || !opts) fail(MAFM_E_INVALID, "null argument");
         *opts = mafm_run_opts{};
         opts->precision = plan->dfp ? MAFM_DF : MAFM_FP32C;
-        opts->lanes_per_column = plan->cfg.lanes;
-        opts->block_threads = plan->cfg.block;
-        opts->columns_per_tile = plan->cfg.cols_per_tile;
+        opts->lanes_per_column = plan->dfp ? plan->df_lanes : plan->cfg.lanes;
+        opts->block_threads = plan->dfp ? 128 : plan->cfg.block;
+        opts->columns_per_tile = plan->dfp ? 1 : plan->cfg.cols_per_tile;
     });
 }
 

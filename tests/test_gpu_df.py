@@ -16,10 +16,13 @@ step-matched filter and no fraction:
   Fz                    within 1e-8 relative (denominator max(|Fz_ref|, 0.01 = ftol);
                         the metric's bar is 1e-3); 1e-6 on the random scans
 
-The FP64 re-relaxation itself (repair64_kernel, one warp per column) must
-reproduce the plain FP64 kernel bit for bit: MAFM_DF_TIE_SCALE widens the
-near-tie margins until every column is re-relaxed, and the result is
-compared with MAFM_FP64 on every field.
+The FP64 re-relaxation itself (one warp per column, inside the double-float
+kernel or in repair64_kernel after it) must reproduce the plain FP64 kernel
+bit for bit: MAFM_DF_TIE_SCALE widens the near-tie margins until every column
+is re-relaxed, and the result is compared with MAFM_FP64 on every field.
+Over a rigid grid the grid is built in double-float and the re-relaxation
+reads its FP64 copy, whose nodes agree with the FP64 build to about 1e-14:
+there the re-relaxed points must equal FP64's steps and lie within 1e-9.
 """
 import ctypes as C
 
@@ -36,8 +39,8 @@ pytestmark = pytest.mark.gpu
 TIP_TOL = 1e-8
 FZ_TOL = 1e-8
 FZ_FLOOR = 0.01
-# every fixture but the two rigid-grid ones (MAFM_DF refuses rigid grids)
-DF_CASES = [n for n in POINT_CASES if n not in ("graphene_grid", "slab_es_grid")]
+DF_CASES = list(POINT_CASES)
+RIGID_CASES = ["graphene_grid", "slab_es_grid"]
 
 
 def run_case(case, precision, **kw):
@@ -78,8 +81,6 @@ def test_df_matches_oracle_on_random_scans(tmp_path):
     specs += [random_periodic_spec(s) for s in range(8)]
     for i, spec in enumerate(specs):
         desc = Input(spec.write(str(tmp_path / f"s{i}"))).desc()
-        if desc.c.rigidgrid:
-            continue
         want, _ = oracle.run(desc)
         scan = Scan(desc, device=0)
         got, _ = scan.run(_abi.DF)
@@ -141,9 +142,46 @@ def test_df_batch_equals_single_runs_and_plan_replays():
     L.mafm_plan_destroy(plan)
 
 
-def test_df_refuses_rigid_grids():
-    case = golden("graphene_grid")
-    scan = Scan(Input(case.input).desc(), device=0)
-    with pytest.raises(_abi.MafmError) as e:
-        scan.run(_abi.DF, col_begin=0, col_end=2)
-    assert e.value.code == _abi.MAFM_E_UNSUPPORTED
+@pytest.mark.parametrize("name", RIGID_CASES)
+def test_fp64_re_relaxation_over_the_df_grid(name, monkeypatch):
+    case = golden(name)
+    want, _ = run_case(case, _abi.FP64)
+    monkeypatch.setenv("MAFM_DF_TIE_SCALE", "1e20")
+    got, n_fp64 = run_case(case, _abi.DF)
+    assert n_fp64 == sum(c1 - c0 for c0, c1 in case.columns(Input(case.input).desc().c.ny))
+    assert np.all(got["status"] & _abi.PT_FP64)
+    assert_faithful(got, want, tip_tol=1e-9, fz_tol=1e-9)
+
+
+def test_df_grid_rebuild_is_identical_and_captures_with_the_plan():
+    """mafm_scan_build_grid(MAFM_DF) rebuilds the double-float grid bit for
+    bit, and a CUDA graph of [grid build, plan launch] replays the run."""
+    import torch
+    case = golden("slab_es_grid")
+    desc = Input(case.input).desc()
+    i0, i1, j0, j1 = case.meta["block"]
+    scan = Scan(desc.crop(i0, j0, i1 - i0, j1 - j0), device=0)
+    first, _ = scan.run(_abi.DF)
+    L = _abi.lib()
+    stream = torch.cuda.Stream()
+    sp = C.c_void_p(stream.cuda_stream)
+    _abi.check(L.mafm_scan_build_grid(scan.handle, _abi.DF, sp))
+    again, _ = scan.run(_abi.DF)
+    np.testing.assert_array_equal(again, first)
+    dev = torch.zeros(scan.desc.n_points * 64, dtype=torch.uint8, device="cuda:0")
+    handles = (C.c_void_p * 1)(scan.handle)
+    optrs = (C.c_void_p * 1)(dev.data_ptr())
+    opts = _abi.RunOpts(_abi.DF, 0, 0, 0, 0, 0)
+    plan = C.c_void_p()
+    _abi.check(L.mafm_plan_create(handles, 1, C.byref(opts), optrs, C.byref(plan)))
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=stream):
+        _abi.check(L.mafm_scan_build_grid(scan.handle, _abi.DF, sp))
+        _abi.check(L.mafm_plan_launch(plan, sp))
+    dev.fill_(0xFF)
+    g.replay()
+    torch.cuda.synchronize()
+    got = np.frombuffer(dev.cpu().numpy().tobytes(), dtype=_abi.POINT_DTYPE)
+    np.testing.assert_array_equal(got, first)
+    L.mafm_plan_destroy(plan)
+    scan.close()

@@ -7,7 +7,8 @@ with a device error bit once a warp runs past MAFM_WATCHDOG_S seconds
 MAFM_E_DEVICE and the context stays usable: the kernel returns normally, it
 never traps.  Each test sets a limit of one microsecond, which every warp
 passes long before its first column is relaxed, expects MAFM_E_DEVICE, and
-then relaxes the same scan again without the limit in the same process.
+then relaxes the same scan again without the limit in the same process
+(FP32C, FP32C batch, double-float and flexible kernels).
 """
 import numpy as np
 import pytest
@@ -44,6 +45,21 @@ def test_fp32c_watchdog_ends_the_kernel_and_the_context_recovers(monkeypatch):
     _same_points(after, before)
     after64, _ = scan.run(_abi.FP64, col_begin=0, col_end=8)
     _same_points(after64, before64)
+    scan.close()
+
+
+def test_df_watchdog_ends_the_kernel_and_the_context_recovers(monkeypatch):
+    case = golden("graphene_ef")
+    scan = Scan(Input(case.input).desc(), device=0)
+    before, _ = scan.run(_abi.DF)
+    monkeypatch.setenv("MAFM_WATCHDOG_S", TINY)
+    with pytest.raises(_abi.MafmError) as e:
+        scan.run(_abi.DF)
+    assert e.value.code == _abi.MAFM_E_DEVICE
+    assert "watchdog" in e.value.msg
+    monkeypatch.delenv("MAFM_WATCHDOG_S")
+    after, _ = scan.run(_abi.DF)
+    _same_points(after, before)
     scan.close()
 
 
