@@ -102,20 +102,11 @@ __device__ __forceinline__ float2 f2(float4 v, int hi) {
     return hi ? make_float2(v.z, v.w) : make_float2(v.x, v.y);
 }
 
-// x^2 + y^2 + z^2: the squares of the high parts exactly (product and FMA
-// residue), the cross terms 2 h l into the low part (l^2 is below 2^-46 of
-// the square), the three high squares added by two_sum.
-__device__ __forceinline__ D2 sumsq_u(D2 x, D2 y, D2 z) {
-    const float2 px = p_mul(x.h, x.h), py = p_mul(y.h, y.h), pz = p_mul(z.h, z.h);
-    float2 ex = p_fma(x.h, x.h, p_neg(px));
-    float2 ey = p_fma(y.h, y.h, p_neg(py));
-    float2 ez = p_fma(z.h, z.h, p_neg(pz));
-    ex = p_fma(p_add(x.h, x.h), x.l, ex);
-    ey = p_fma(p_add(y.h, y.h), y.l, ey);
-    ez = p_fma(p_add(z.h, z.h), z.l, ez);
-    const D2 s1 = dfl2_two_sum(px, py);
-    const D2 s2 = dfl2_two_sum(s1.h, pz);
-    return {s2.h, p_add(p_add(p_add(ex, ey), p_add(ez, s1.l)), s2.l)};
+// x^2: the square of the high part exactly (product and FMA residue), the
+// cross term 2 h l into the low part (l^2 is below 2^-46 of the square).
+__device__ __forceinline__ D2 sq_u(D2 x) {
+    const float2 p = p_mul(x.h, x.h);
+    return {p, p_fma(p_add(x.h, x.h), x.l, p_fma(x.h, x.h, p_neg(p)))};
 }
 
 // 1 / sqrt(a) as dfl2_rsqrt, for an operand that need not be normalised
@@ -126,41 +117,62 @@ __device__ __forceinline__ D2 rsqrt_u(D2 a) {
     return dfl2_fast_two_sum(y, p_mul(p_mul(y, e), p_bcast(0.5f)));
 }
 
-// The packed form of pair_df: the two terms of a record, of kind KIND, at
-// once; their forces and energies go into the lazy sums.
+// The two terms of a TermPairDF record (element .x the first, .y the second).
+struct PairDF2 {
+    D2 x, y, z, qq, p0, p1, p2;
+    int coul;
+};
+
 template <int KIND>
-__device__ __forceinline__ void pair_df2(const TermPairDF* rec, D2 tx, D2 ty, D2 tz, LazySum2& fx,
-                                         LazySum2& fy, LazySum2& fz, LazySum2& ee) {
+__device__ __forceinline__ PairDF2 load_pair(const TermPairDF* rec) {
     const float4* q = reinterpret_cast<const float4*>(rec);
     const float4 a = __ldg(q), b = __ldg(q + 1), c = __ldg(q + 2), g = __ldg(q + 3);
     const float4 h = __ldg(q + 4), m = __ldg(q + 5);
-    const int coul = __float_as_int(__ldg(reinterpret_cast<const float*>(q + 7)));
-    const D2 dx = dfl2_sub_u(tx, D2{f2(a, 0), f2(a, 1)});
-    const D2 dy = dfl2_sub_u(ty, D2{f2(b, 0), f2(b, 1)});
-    const D2 dz = dfl2_sub_u(tz, D2{f2(c, 0), f2(c, 1)});
-    const D2 p0 = {f2(h, 0), f2(h, 1)}, p1 = {f2(m, 0), f2(m, 1)};
-    const D2 r2 = sumsq_u(dx, dy, dz);
+    PairDF2 t;
+    t.x = {f2(a, 0), f2(a, 1)};
+    t.y = {f2(b, 0), f2(b, 1)};
+    t.z = {f2(c, 0), f2(c, 1)};
+    t.qq = {f2(g, 0), f2(g, 1)};
+    t.p0 = {f2(h, 0), f2(h, 1)};
+    t.p1 = {f2(m, 0), f2(m, 1)};
+    if (KIND == MAFM_PAIR_MORSE) {
+        const float4 n = __ldg(q + 6);
+        t.p2 = {f2(n, 0), f2(n, 1)};
+    } else {
+        t.p2 = {p_bcast(0.0f), p_bcast(0.0f)};
+    }
+    t.coul = __float_as_int(__ldg(reinterpret_cast<const float*>(q + 7)));
+    return t;
+}
+
+// LJ (interactions.cpp:15-27) or Morse (:29-40), plus Coulomb (:42-51) when
+// the record has one, for the separation d = tip - atom with r2 = |d|^2; the
+// force on the tip and the energy go into the lazy sums.  1/r comes from a
+// double-float rsqrt.
+template <int KIND>
+__device__ __forceinline__ void pair_df2_at(const PairDF2& t, D2 dx, D2 dy, D2 dz, D2 r2, LazySum2& fx,
+                                            LazySum2& fy, LazySum2& fz, LazySum2& ee) {
     const D2 ir = rsqrt_u(r2);
     const D2 ir2 = dfl2_mul_u(ir, ir);
     D2 e, s;
     if (KIND == MAFM_PAIR_LJ) {
         const D2 ir6 = dfl2_norm(dfl2_mul_u(dfl2_mul_u(ir2, ir2), ir2));
-        const D2 ta = dfl2_mul_u(p1, dfl2_mul_u(ir6, ir6));   // es12 / r^12
-        const D2 tb = dfl2_mul_u(p0, ir6);               // es6 / r^6
+        const D2 ta = dfl2_mul_u(t.p1, dfl2_mul_u(ir6, ir6));   // es12 / r^12
+        const D2 tb = dfl2_mul_u(t.p0, ir6);                   // es6 / r^6
         e = dfl2_sub_u(ta, tb);
         s = dfl2_mul_u(dfl2_sub_u(dfl2_mulf_u(ta, p_bcast(12.0f)), dfl2_mulf_u(tb, p_bcast(6.0f))), ir2);
     } else {
-        const float4 n = __ldg(q + 6);
-        const D2 p2 = {f2(n, 0), f2(n, 1)};
-        const D2 r = r2 * ir;
-        const D2 qe = dfl2_exp(-(p1 * (r - p2)));
-        const D2 qe2 = qe * qe;
-        e = p0 * ((qe2 - qe * 2.0f) + D2{p_bcast(1.0f), p_bcast(0.0f)});
-        s = ((p0 * p1) * 2.0f) * (qe2 - qe) * ir;
+        const D2 r = dfl2_mul_u(r2, ir);
+        const D2 qe = dfl2_exp(-dfl2_mul_u(t.p1, dfl2_sub_u(r, t.p2)));
+        const D2 qe2 = dfl2_mul_u(qe, qe);
+        // De (q^2 - 2 q + 1), 2 De a (q^2 - q) / r
+        e = dfl2_mul_u(t.p0, dfl2_add_u(dfl2_sub_u(qe2, dfl2_mulf_u(qe, p_bcast(2.0f))),
+                                        D2{p_bcast(1.0f), p_bcast(0.0f)}));
+        s = dfl2_mul_u(dfl2_mul_u(dfl2_mulf_u(dfl2_mul_u(t.p0, t.p1), p_bcast(2.0f)),
+                                  dfl2_sub_u(qe2, qe)), ir);
     }
-    if (coul) {
-        const D2 qq = {f2(g, 0), f2(g, 1)};
-        const D2 ec = dfl2_mul_u(qq, ir);
+    if (t.coul) {
+        const D2 ec = dfl2_mul_u(t.qq, ir);
         e = dfl2_add_u(e, ec);
         s = dfl2_add_u(s, dfl2_mul_u(ec, ir2));
     }
@@ -168,6 +180,16 @@ __device__ __forceinline__ void pair_df2(const TermPairDF* rec, D2 tx, D2 ty, D2
     fy.add(dfl2_mul_u(s, dy));
     fz.add(dfl2_mul_u(s, dz));
     ee.add(e);
+}
+
+// The two terms of a record at the tip (tx, ty, tz).
+template <int KIND>
+__device__ __forceinline__ void pair_df2(const TermPairDF* rec, D2 tx, D2 ty, D2 tz, LazySum2& fx,
+                                         LazySum2& fy, LazySum2& fz, LazySum2& ee) {
+    const PairDF2 t = load_pair<KIND>(rec);
+    const D2 dx = dfl2_sub_u(tx, t.x), dy = dfl2_sub_u(ty, t.y), dz = dfl2_sub_u(tz, t.z);
+    const D2 r2 = dfl2_add_u(dfl2_add_u(sq_u(dx), sq_u(dy)), sq_u(dz));
+    pair_df2_at<KIND>(t, dx, dy, dz, r2, fx, fy, fz, ee);
 }
 
 // ForceGrid::interpolate (force_grid.cpp:88-155) on the double-float copy of
@@ -567,7 +589,7 @@ __global__ void __launch_bounds__(128) relaxdf_kernel(const BatchDF* __restrict_
             s.vel = {v.x + dt * F.x, v.y + dt * F.y, v.z + dt * F.z};
             step_done = true;
         } else if (P.integrator == MAFM_INT_MIDPOINT) {
-            const D h = dt / D(2);
+            const D h(__fmul_rn(dt.h, 0.5f), __fmul_rn(dt.l, 0.5f));   // dt / 2, exactly
             if (s.phase == DF_EVAL0) {
                 const V3D pp = s.tip, v = s.vel;
                 s.ex = {pp.x + h * v.x, pp.y + h * v.y, pp.z + h * v.z};
@@ -580,7 +602,7 @@ __global__ void __launch_bounds__(128) relaxdf_kernel(const BatchDF* __restrict_
                 step_done = true;
             }
         } else {   // RK4
-            const D h = dt / D(2);
+            const D h(__fmul_rn(dt.h, 0.5f), __fmul_rn(dt.l, 0.5f));   // dt / 2, exactly
             const V3D pp = s.tip, v = s.vel;
             if (s.phase == DF_EVAL0) {
                 s.fs = F; s.es = E; s.vs = v;
@@ -601,10 +623,11 @@ __global__ void __launch_bounds__(128) relaxdf_kernel(const BatchDF* __restrict_
                 s.es = s.es + E;
                 s.vs = {s.vs.x + s.u.x, s.vs.y + s.u.y, s.vs.z + s.u.z};
                 const D s6 = dt / D(6);
+                const D sixth = D(1.0 / 6.0);
                 s.tip = {pp.x + s6 * s.vs.x, pp.y + s6 * s.vs.y, pp.z + s6 * s.vs.z};
                 s.vel = {v.x + s6 * s.fs.x, v.y + s6 * s.fs.y, v.z + s6 * s.fs.z};
-                SF = {s.fs.x / D(6), s.fs.y / D(6), s.fs.z / D(6)};
-                SE = s.es / D(6);
+                SF = {s.fs.x * sixth, s.fs.y * sixth, s.fs.z * sixth};
+                SE = s.es * sixth;
                 step_done = true;
             }
         }
@@ -644,7 +667,10 @@ __global__ void __launch_bounds__(128) relaxdf_kernel(const BatchDF* __restrict_
             const V3D w = s.vel;
             const D pw = w.x * SF.x + w.y * SF.y + w.z * SF.z;
             V3D fh = {D(0), D(0), D(0)};
-            if (fl > D(1e-10)) fh = {SF.x / fl, SF.y / fl, SF.z / fl};
+            if (fl > D(1e-10)) {
+                const D ifl = dfl_rcp(fl);
+                fh = {SF.x * ifl, SF.y * ifl, SF.z * ifl};
+            }
             const D vl = len3(w);
             s.tie |= dfl_fabs(pw) < vl * (P.tie.p_f + P.tie.p_v * fl);
             if (s.tie && repair_list) {
@@ -730,29 +756,61 @@ __global__ void nodes_to_df_kernel(const Node64* in, NodeDF* out, long long n) {
 }
 
 // Simulation::buildTipGridInteractions (simulation.cpp:420-501) in
-// double-float: one thread per node (z fastest, so a warp's nodes share x and
-// y and read the same term records), the tip on the node (the node's x and y
-// wrapped into the cell under tip_pbc, as temp_system does, :462-464), every
-// tip–surface term of p (ts_mode 1: with the external field).
+// double-float.  One thread per strip of NB consecutive nodes of a grid
+// column (z fastest, so a warp's strips share x and y and read the same term
+// records): the tip on each node (the node's x and y wrapped into the cell
+// under tip_pbc, as temp_system does, :462-464), every tip–surface term of p
+// (ts_mode 1: with the external field).  The x and y separations of a record
+// and their squares are formed once for the strip.
+template <int NB>
 __global__ void __launch_bounds__(128) grid_builddf_kernel(const ScanParamsDF p, NodeDF* out,
                                                            unsigned* err_word) {
     const GridViewDF& g = p.grid;
-    const long long total = (long long)g.n[0] * g.n[1] * g.n[2];
+    const int nzs = (g.n[2] + NB - 1) / NB;
+    const long long total = (long long)g.n[0] * g.n[1] * nzs;
+    const int n_lj = p.n_lj_pairs, n_all = p.n_lj_pairs + p.n_morse_pairs;
     unsigned err = 0;
     for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
          idx += (long long)gridDim.x * blockDim.x) {
-        const int k = (int)(idx % g.n[2]);
-        const long long ij = idx / g.n[2];
+        const int k0 = (int)(idx % nzs) * NB;
+        const long long ij = idx / nzs;
         const int j = (int)(ij % g.n[1]), i = (int)(ij / g.n[1]);
         D x, y;
         dummy_xy_t(p, p.tip_pbc != 0, D(i) * g.basis[0] + g.origin[0], D(j) * g.basis[4] + g.origin[1],
                    x, y);
-        const V3D tip = {x, y, D(k) * g.basis[8] + g.origin[2]};
-        V3D F;
-        D E;
-        int unused = 0;
-        ts_df<1>(p, tip, 0, 1u, F, E, unused, err);
-        out[idx] = NodeDF{F.x, F.y, F.z, E};
+        const D2 tx = dfl2(x), ty = dfl2(y);
+        D2 tz[NB];
+#pragma unroll
+        for (int m = 0; m < NB; ++m) tz[m] = dfl2(D(k0 + m) * g.basis[8] + g.origin[2]);
+        LazySum2 fx[NB], fy[NB], fz[NB], ee[NB];
+#pragma unroll 1
+        for (int r = 0; r < n_all; ++r) {
+            const bool lj = r < n_lj;
+            const PairDF2 t = lj ? load_pair<MAFM_PAIR_LJ>(p.pairs + r) : load_pair<MAFM_PAIR_MORSE>(p.pairs + r);
+            const D2 dx = dfl2_sub_u(tx, t.x), dy = dfl2_sub_u(ty, t.y);
+            const D2 dxy2 = dfl2_add_u(sq_u(dx), sq_u(dy));
+#pragma unroll
+            for (int m = 0; m < NB; ++m) {
+                const D2 dz = dfl2_sub_u(tz[m], t.z);
+                const D2 r2 = dfl2_add_u(dxy2, sq_u(dz));
+                if (lj) pair_df2_at<MAFM_PAIR_LJ>(t, dx, dy, dz, r2, fx[m], fy[m], fz[m], ee[m]);
+                else pair_df2_at<MAFM_PAIR_MORSE>(t, dx, dy, dz, r2, fx[m], fy[m], fz[m], ee[m]);
+            }
+        }
+#pragma unroll
+        for (int m = 0; m < NB; ++m) {
+            if (k0 + m >= g.n[2]) break;
+            V3D F = {fx[m].value(), fy[m].value(), fz[m].value()};
+            D E = ee[m].value();
+            if (p.ts_mode == 1) {
+                V3D f;
+                D e;
+                interp_df(p.es, V3D{x, y, D(k0 + m) * g.basis[8] + g.origin[2]}, f, e);
+                F = {F.x + f.x, F.y + f.y, F.z + f.z};
+                E = E + e;
+            }
+            out[ij * g.n[2] + k0 + m] = NodeDF{F.x, F.y, F.z, E};
+        }
     }
     if (err) atomicOr(err_word, err);
 }
@@ -944,12 +1002,14 @@ cudaError_t launch_grid_builddf(const ScanParamsDF& p, NodeDF* out, Node64* out6
     if (n <= 0) return cudaSuccess;
     ScanParamsDF q = p;
     q.grid.g = out;
+    constexpr int kNB = 4;
+    const long long strips = (long long)p.grid.n[0] * p.grid.n[1] * ((p.grid.n[2] + kNB - 1) / kNB);
     int per_sm = 0;
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, grid_builddf_kernel, 128, 0);
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, grid_builddf_kernel<kNB>, 128, 0);
     if (e != cudaSuccess) return e;
     if (per_sm <= 0) per_sm = 1;
-    const long long blocks = std::max(1ll, std::min((n + 127) / 128, (long long)sm_count() * per_sm * 8));
-    grid_builddf_kernel<<<(unsigned)blocks, 128, 0, s>>>(q, out, err_word);
+    const long long blocks = std::max(1ll, std::min((strips + 127) / 128, (long long)sm_count() * per_sm * 8));
+    grid_builddf_kernel<kNB><<<(unsigned)blocks, 128, 0, s>>>(q, out, err_word);
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     const long long b64 = std::min((n + 255) / 256, (long long)sm_count() * 32);
