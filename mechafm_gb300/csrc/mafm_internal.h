@@ -158,7 +158,8 @@ struct RunCounters {
     unsigned int error_word;
     unsigned int n_tie;               // MAFM_DF: columns listed for FP64 re-relaxation
                                       // (may exceed the list's capacity)
-    unsigned long long repair_next;   // queue head of the re-relaxation kernel
+    unsigned long long repair_next;   // queue head of the FP64 re-relaxation (taken in the
+                                      // double-float kernel, then by repair64_kernel)
 };
 
 // Launchers implemented in relax64.cu / relax32.cu.  ctr points to zeroed
