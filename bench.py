@@ -75,9 +75,18 @@ BYTES_LOOKUP = 8 * 16
 # 200 x 200 px slab launch: the grid nodes read once and the output records
 # written (gathers within a column are served by L1 and L2).
 DRAM_BYTES_PER_LOOKUP = 351.3e6 / 190890530
-# Output bytes of one relaxed point (the 64 B mafm_point record); the relax
-# kernels' DRAM traffic is these records, written once.
+# Output bytes of one relaxed point (the 64 B mafm_point record), written once.
 POINT_BYTES = 64
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per relaxed point of
+# the relax kernels, from ncu captures of one 285 x 285 x 41 cluster launch
+# (3,330,225 points): relaxdf_kernel 13.0 + 180.4 MB, relax32_kernel 6.0 +
+# 165.9 MB.  The output records are the traffic; the last of them can still
+# sit in the 126 MB L2 when the capture ends, so these are lower bounds.
+DRAM_BYTES_PER_POINT_DF = 193.4e6 / 3330225
+DRAM_BYTES_PER_POINT_32 = 171.9e6 / 3330225
+# DRAM bytes per node of grid_builddf_kernel: ncu of one 64 x 64 px slab grid
+# (3,475,509 nodes): 9.5 + 57.1 MB (a lower bound, as above).
+DRAM_BYTES_PER_NODE_DF = 66.6e6 / 3475509
 CPU_TARGET_S = 10.0        # CPU sample length
 RIGID_CROP = 16            # pixels per side of the rigid-grid CPU sample
 FP64_RIGID_CROP = 64       # pixels per side of the rigid-grid FP64 comparison
@@ -890,9 +899,12 @@ def ours(args, rank, world, local):
         kname = "relaxdf_kernel + repair64_kernel" if head == _abi.DF else "relax32_kernel"
         if fpe.any():
             relax_line = fp32_roofline(relax_flops / (ms_relax / 1000.0) / 1e12, peak_tflops, {
-                "traffic": POINT_BYTES * n_pts,
-                "traffic_source": "algorithmic output bytes (64 B per point, written once); the "
-                                  "ncu captures in profiles/ measure the DRAM bytes per point",
+                "traffic": (DRAM_BYTES_PER_POINT_DF if head == _abi.DF else DRAM_BYTES_PER_POINT_32) * n_pts,
+                "traffic_source": ("ncu dram__bytes_read.sum + dram__bytes_write.sum of one 285x285x41 "
+                                   "cluster launch, scaled by points; a lower bound (the capture's last "
+                                   "output records can stay in L2); algorithmic bytes: the 64 B output "
+                                   "record per point"),
+                "algorithmic_bytes": POINT_BYTES * n_pts,
                 "kernel": kname, "kernel_ms": ms_relax,
                 "kernel_ms_source": ("events recorded inside the timed graph replays"
                                      if step.external else
@@ -956,6 +968,9 @@ def ours(args, rank, world, local):
                                                              " (MAFM_FP32C, the fast path)")),
                          "kernel_ms": ms_b, "nodes": nodes, "flops_per_node": float(fl / nodes)}
                 if df:
+                    extra["traffic"] = DRAM_BYTES_PER_NODE_DF * nodes
+                    extra["traffic_source"] = ("ncu dram__bytes of one 64x64 px slab grid build "
+                                               "(3,475,509 nodes), scaled by nodes; a lower bound")
                     f64 = flops64 / (ms_b / 1000.0) / 1e12
                     extra["flops_source"] = (f"double-float FP32 operations per term: LJ {DF_FLOPS_LJ}, "
                                              f"Morse {DF_FLOPS_MORSE}, Coulomb {DF_FLOPS_COUL}")
