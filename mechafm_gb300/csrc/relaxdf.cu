@@ -933,10 +933,11 @@ constexpr size_t kDfSmem = (size_t)(128 / 32) * 2 * kWarpChunk * sizeof(Node64);
 
 // Default: one lane per column while the columns fill the resident lanes;
 // fewer columns share out their terms, G = the largest power of two up to 8
-// with G x columns <= resident lanes.  Measured (MAFM_DF_LANES overrides):
-// 401 x 401 cluster (160,801 columns, 58,368 resident lanes) G = 1 / 2 / 4 /
-// 8: 768 / 823 / 935 / 1627 ms; 101 x 101 graphene (10,201 columns):
-// 144 / 125 / 112 / 153 ms.
+// with G x columns <= 1.25 x the resident lanes.  Measured (MAFM_DF_LANES
+// overrides), G = 1 / 2 / 4 / 8: 401 x 401 cluster (160,801 columns, 58,368
+// resident lanes) 768 / 823 / 935 / 1627 ms; 128 x 128 cluster (16,384
+// columns) 183 / 162 / 142 / 182 ms; 101 x 101 graphene (10,201 columns)
+// 147 / 129 / 111 / 158 ms.
 int df_lanes_per_column(long long n_cols, int requested) {
     if (requested == 1 || requested == 2 || requested == 4 || requested == 8) return requested;
     if (const char* e = std::getenv("MAFM_DF_LANES")) {
@@ -949,7 +950,7 @@ int df_lanes_per_column(long long n_cols, int requested) {
         per_sm = 1;
     const long long lanes = (long long)sm_count() * per_sm * 128;
     int g = 1;
-    while (g < 8 && n_cols > 0 && 2 * g * n_cols <= lanes) g *= 2;
+    while (g < 8 && n_cols > 0 && 4 * (2 * g * n_cols) <= 5 * lanes) g *= 2;
     return g;
 }
 
