@@ -123,3 +123,37 @@ def test_cli_stdout_matches_reference_executable(name, tmp_path):
     assert fin[:len(fin_ref)] == fin_ref
     assert len(mid) == len(wrote) + len(fin)
 
+
+
+@pytest.mark.gpu
+def test_cli_rigid_grid_default_matches_fp64(tmp_path):
+    """A rigid-grid scan through the executable: the default (double-float
+    grid build and relaxation) against MAFM_PRECISION=fp64 (the FP64 grid
+    and kernel), row for row, within one unit of the last printed digit and
+    with equal step counts."""
+    folder = os.path.join(GOLDEN, "graphene_grid")
+    inp = os.path.join(folder, MANIFEST["graphene_grid"]["input"])
+    rows = {}
+    for prec in ("", "fp64"):
+        out = str(tmp_path / f"out_{prec or 'df'}") + "/"
+        env = dict(os.environ)
+        env.pop("MAFM_PRECISION", None)
+        if prec:
+            env["MAFM_PRECISION"] = prec
+        r = subprocess.run([CLI, inp, out], cwd=folder, capture_output=True, text=True, timeout=600,
+                           env=env)
+        assert r.returncode == 0, r.stderr[-2000:]
+        lines = []
+        for fn in sorted(os.listdir(out)):
+            if fn.startswith("scan-"):
+                lines += [fn + "\t" + l.rstrip("\n") for l in open(os.path.join(out, fn))]
+        path = tmp_path / f"rows_{prec or 'df'}.txt"
+        path.write_text("\n".join(lines) + "\n")
+        rows[prec] = _rows(str(path))
+    got, want = rows[""], rows["fp64"]
+    assert got.keys() == want.keys() and len(want) == MANIFEST["graphene_grid"]["points"]
+    tol = np.array([1e-3] * 3 + [1e-4] * 3 + [1e-3] * 4 + [1e-4] * 2)
+    for key in want:
+        g, w = np.array(got[key]), np.array(want[key])
+        assert (np.abs(g[:-1] - w[:-1]) <= tol + 1e-9).all(), (key, g, w)
+        assert g[-1] == w[-1], (key, g[-1], w[-1])
