@@ -65,7 +65,12 @@ FLOPS_LJ, FLOPS_MORSE, FLOPS_COUL = 25, 29, 20
 # FP32 operations (FMA = 2) of one term in the double-float kernel, counted
 # from its source (pair_df2 and the dfloat2 operations it calls): the work of
 # the double-float algorithms that compute the FP64-faithful term.
-DF_FLOPS_LJ, DF_FLOPS_MORSE, DF_FLOPS_COUL = 206, 475, 30
+# A Coulomb term costs less beside an LJ term (their 1/r^2 factors merge).
+DF_FLOPS_LJ, DF_FLOPS_MORSE, DF_FLOPS_COUL_LJ, DF_FLOPS_COUL_MORSE = 201, 475, 23, 30
+DF_TABLE = (DF_FLOPS_LJ, DF_FLOPS_MORSE, DF_FLOPS_COUL_LJ, DF_FLOPS_COUL_MORSE)
+DF_TABLE_TEXT = (f"double-float FP32 operations (FMA = 2) per term, counted from the kernel source: "
+                 f"LJ {DF_FLOPS_LJ}, Morse {DF_FLOPS_MORSE}, Coulomb {DF_FLOPS_COUL_LJ} beside LJ "
+                 f"and {DF_FLOPS_COUL_MORSE} beside Morse")
 # GB300's nominal FP64 rate (MEASURED_PEAKS.json measures HBM and bf16 only).
 FP64_PEAK_NOMINAL_TFLOPS = 1.25
 # Algorithmic bytes of one trilinear lookup: 8 FP32 {F, E} nodes.
@@ -156,10 +161,11 @@ def make_inputs(name, tmp, pixels=0):
     return inputs, WORKLOADS[name]
 
 
-def term_flops(desc, direct: bool = False, table=(FLOPS_LJ, FLOPS_MORSE, FLOPS_COUL)):
+def term_flops(desc, direct: bool = False, table=(FLOPS_LJ, FLOPS_MORSE, FLOPS_COUL, FLOPS_COUL)):
     """Algorithmic flops of one force evaluation over a scan's tip–atom terms
     (direct=True: the terms a rigid-grid node samples); table = flops of an
-    LJ, a Morse and a Coulomb term (the FP64 expressions' by default)."""
+    LJ term, a Morse term, and a Coulomb term beside an LJ or a Morse term
+    (the FP64 expressions' by default)."""
     from mechafm_gb300 import _abi
     if desc.c.rigidgrid and not direct:
         return 0
@@ -168,8 +174,10 @@ def term_flops(desc, direct: bool = False, table=(FLOPS_LJ, FLOPS_MORSE, FLOPS_C
     images = 9 if desc.c.vdw_pbc else 1
     n_lj = int((kinds == _abi.PAIR_LJ).sum()) * images
     n_mo = int((kinds == _abi.PAIR_MORSE).sum()) * images
-    n_co = int(((a["charge"] != 0) & bool(desc.c.coulomb) & (desc.c.tip_charge != 0)).sum())
-    return n_lj * table[0] + n_mo * table[1] + n_co * table[2]
+    charged = (a["charge"] != 0) & bool(desc.c.coulomb) & (desc.c.tip_charge != 0)
+    n_co_lj = int((charged & (kinds == _abi.PAIR_LJ)).sum())
+    n_co_mo = int((charged & (kinds == _abi.PAIR_MORSE)).sum())
+    return n_lj * table[0] + n_mo * table[1] + n_co_lj * table[2] + n_co_mo * table[3]
 
 
 def rigid_nodes(d) -> int:
@@ -914,16 +922,13 @@ def ours(args, rank, world, local):
             if head == _abi.DF:
                 # the kernel computes in double-float: its algorithmic work is
                 # the FP32 operations of the double-float term algorithms
-                fpe_df = np.array([term_flops(d, table=(DF_FLOPS_LJ, DF_FLOPS_MORSE, DF_FLOPS_COUL))
-                                   for d in descs], dtype=float)
+                fpe_df = np.array([term_flops(d, table=DF_TABLE) for d in descs], dtype=float)
                 df_per_eval = float((wts * fpe_df).sum() / wts.sum())
                 fp64_equiv = relax_flops / (ms_relax / 1000.0) / 1e12
                 relax_line["achieved"] = st.force_evals * df_per_eval / (ms_relax / 1000.0) / 1e12
                 relax_line["frac"] = relax_line["achieved"] / peak_tflops
                 relax_line["flops_per_force_eval"] = df_per_eval
-                relax_line["flops_source"] = (
-                    f"double-float FP32 operations (FMA = 2) per term, counted from the kernel "
-                    f"source: LJ {DF_FLOPS_LJ}, Morse {DF_FLOPS_MORSE}, Coulomb {DF_FLOPS_COUL}")
+                relax_line["flops_source"] = DF_TABLE_TEXT
                 relax_line["fp64_equivalent"] = {
                     "flops_per_force_eval": float((wts * fpe).sum() / wts.sum()),
                     "achieved_tflops": fp64_equiv,
@@ -959,8 +964,7 @@ def ours(args, rank, world, local):
             flops64 = sum(rigid_nodes(s.desc.c) * term_flops(s.desc, direct=True) for s in rigid)
 
             def build_line(ms_b, df):
-                tbl = (DF_FLOPS_LJ, DF_FLOPS_MORSE, DF_FLOPS_COUL) if df else (FLOPS_LJ, FLOPS_MORSE,
-                                                                            FLOPS_COUL)
+                tbl = DF_TABLE if df else (FLOPS_LJ, FLOPS_MORSE, FLOPS_COUL, FLOPS_COUL)
                 fl = sum(rigid_nodes(s.desc.c) * term_flops(s.desc, direct=True, table=tbl)
                          for s in rigid)
                 extra = {"kernel": ("grid_builddf_kernel (+ its FP64 copy)" if df else
@@ -972,8 +976,7 @@ def ours(args, rank, world, local):
                     extra["traffic_source"] = ("ncu dram__bytes of one 64x64 px slab grid build "
                                                "(3,475,509 nodes), scaled by nodes; a lower bound")
                     f64 = flops64 / (ms_b / 1000.0) / 1e12
-                    extra["flops_source"] = (f"double-float FP32 operations per term: LJ {DF_FLOPS_LJ}, "
-                                             f"Morse {DF_FLOPS_MORSE}, Coulomb {DF_FLOPS_COUL}")
+                    extra["flops_source"] = DF_TABLE_TEXT
                     extra["fp64_equivalent"] = {"achieved_tflops": f64,
                                                 "vs_fp64_peak_nominal": f64 / FP64_PEAK_NOMINAL_TFLOPS}
                 return fp32_roofline(fl / (ms_b / 1000.0) / 1e12, peak_tflops, extra)

@@ -156,11 +156,20 @@ __device__ __forceinline__ void pair_df2_at(const PairDF2& t, D2 dx, D2 dy, D2 d
     const D2 ir2 = dfl2_mul_u(ir, ir);
     D2 e, s;
     if (KIND == MAFM_PAIR_LJ) {
+        // A = es12 / r^6, u = A - es6: E = u / r^6 = es12 / r^12 - es6 / r^6 and
+        // (12 es12 / r^12 - 6 es6 / r^6) / r^2 = 6 (A + u) / r^6 / r^2; the
+        // Coulomb term's qq / r^3 = (qq / r) / r^2 joins before the last / r^2
         const D2 ir6 = dfl2_norm(dfl2_mul_u(dfl2_mul_u(ir2, ir2), ir2));
-        const D2 ta = dfl2_mul_u(t.p1, dfl2_mul_u(ir6, ir6));   // es12 / r^12
-        const D2 tb = dfl2_mul_u(t.p0, ir6);                   // es6 / r^6
-        e = dfl2_sub_u(ta, tb);
-        s = dfl2_mul_u(dfl2_sub_u(dfl2_mulf_u(ta, p_bcast(12.0f)), dfl2_mulf_u(tb, p_bcast(6.0f))), ir2);
+        const D2 A = dfl2_mul_u(t.p1, ir6);
+        const D2 u = dfl2_sub_u(A, t.p0);
+        e = dfl2_mul_u(ir6, u);
+        D2 sr = dfl2_mulf_u(dfl2_mul_u(dfl2_add_u(A, u), ir6), p_bcast(6.0f));
+        if (t.coul) {
+            const D2 ec = dfl2_mul_u(t.qq, ir);
+            e = dfl2_add_u(e, ec);
+            sr = dfl2_add_u(sr, ec);
+        }
+        s = dfl2_mul_u(sr, ir2);
     } else {
         const D2 r = dfl2_mul_u(r2, ir);
         const D2 qe = dfl2_exp(-dfl2_mul_u(t.p1, dfl2_sub_u(r, t.p2)));
@@ -171,7 +180,7 @@ __device__ __forceinline__ void pair_df2_at(const PairDF2& t, D2 dx, D2 dy, D2 d
         s = dfl2_mul_u(dfl2_mul_u(dfl2_mulf_u(dfl2_mul_u(t.p0, t.p1), p_bcast(2.0f)),
                                   dfl2_sub_u(qe2, qe)), ir);
     }
-    if (t.coul) {
+    if (KIND == MAFM_PAIR_MORSE && t.coul) {
         const D2 ec = dfl2_mul_u(t.qq, ir);
         e = dfl2_add_u(e, ec);
         s = dfl2_add_u(s, dfl2_mul_u(ec, ir2));
