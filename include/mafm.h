@@ -322,12 +322,15 @@ int mafm_run_batch(mafm_scan* const* scans, int32_t n_scans, const mafm_run_opts
 int mafm_run_batch_noalloc(mafm_scan* const* scans, int32_t n_scans, const mafm_run_opts* opts,
                            mafm_point* const* outs, mafm_run_stats* stats, void* stream);
 
-/* A prepared batched FP32C relaxation (the same persistent launch as
- * mafm_run_batch) whose per-scan descriptors are uploaded once, so that the
- * launch itself allocates nothing, never synchronises and can be replayed or
- * captured in a CUDA graph.  Replaces the pixel loop of Simulation::run
- * (simulation.cpp:78-122) for many scans at once.  outs must be device memory
- * and stay valid for the plan's lifetime. */
+/* A prepared batched relaxation (MAFM_FP32C or MAFM_DF; the same persistent
+ * launch as mafm_run_batch) whose per-scan descriptors are uploaded once, so
+ * that the launch itself allocates nothing, never synchronises and can be
+ * replayed or captured in a CUDA graph.  Replaces the pixel loop of
+ * Simulation::run (simulation.cpp:78-122) for many scans at once.  Creating a
+ * plan also orders each scan's columns by measured cost (one FP32C
+ * relaxation of the scan, once per scan; the launch then ends with fewer
+ * idle lanes).  outs must be device memory and stay valid for the plan's
+ * lifetime. */
 int mafm_plan_create(mafm_scan* const* scans, int32_t n_scans, const mafm_run_opts* opts,
                      mafm_point* const* outs, mafm_plan** out);
 /* Enqueue one relaxation of every scan of the plan on stream. */
