@@ -487,14 +487,6 @@ def fp64_reference(scans, descs, dev):
         f"by points x atoms")
 
 
-def pick(points, cols, nz):
-    """The points of the listed columns from a whole-scan array."""
-    if cols is None:
-        return points
-    idx = (cols[:, None].astype(np.int64) * nz + np.arange(nz)[None, :]).reshape(-1)
-    return points[idx]
-
-
 def fp32_peak(dev):
     """FP32 CUDA-core throughput: best of 5 FP32 GEMMs with TF32 disabled."""
     import torch
@@ -653,8 +645,31 @@ def ours(args, rank, world, local):
         bufs = [torch.empty(d.n_points * 64, dtype=torch.uint8, device=f"cuda:{dev}") for d in descs]
         return bufs, (C.c_void_p * n)(*[o.data_ptr() for o in bufs])
 
-    def host_points(bufs):
-        return [np.frombuffer(b.cpu().numpy().tobytes(), dtype=_abi.POINT_DTYPE) for b in bufs]
+    def host_points(bufs, refs=None):
+        """Point records of device buffers on the host: whole scans, or only the
+        listed columns of each (gathered on the device first)."""
+        got = []
+        for k, b in enumerate(bufs):
+            cols = refs[k][1] if refs is not None else None
+            if cols is not None:
+                nzk = descs[k].c.nz
+                idx = torch.from_numpy((cols[:, None].astype(np.int64) * nzk +
+                                        np.arange(nzk)[None, :]).reshape(-1)).to(b.device)
+                b = b.view(-1, POINT_BYTES).index_select(0, idx).reshape(-1)
+            got.append(np.frombuffer(b.cpu().numpy().tobytes(), dtype=_abi.POINT_DTYPE))
+        return got
+
+    def record_evals(bufs):
+        """Force evaluations per scan from its point records: FIRE steps x the
+        integrator's evaluations per step (SD, euler 1, midpoint 2, rk4 4),
+        plus each point's output evaluation."""
+        ev = []
+        for b, d in zip(bufs, descs):
+            steps = b.view(torch.int32).view(-1, POINT_BYTES // 4)[:, 14].to(torch.int64).sum().item()
+            per = (1 if d.c.minimiser == _abi.MIN_SD else
+                   {_abi.INT_EULER: 1, _abi.INT_MIDPOINT: 2, _abi.INT_RK4: 4}[d.c.integrator])
+            ev.append(steps * per + d.n_points)
+        return np.array(ev, dtype=float)
 
     # Rigid grids: the first build allocates (outside the timing); a step rebuilds.
     t_grid = 0.0
@@ -875,18 +890,18 @@ def ours(args, rank, world, local):
         # reference on LJ/Coulomb terms)
         fp64 = None
         if not args.no_fp64:
-            head_pts = host_points(outs)
-            fast_pts = host_points(outs32) if outs32 is not None else None
             refs, rate64, npts64, subset = fp64_reference(scans, descs, dev)
+            if not rigid:
+                head_pts = host_points(outs, refs)
+                fast_pts = host_points(outs32, refs) if outs32 is not None else None
             if rigid:
                 # the crop's own relaxations (each precision over its own grid)
                 cmp_head = np.concatenate([s.run(head)[0] for s, _, _ in refs])
                 cmp_fast = (np.concatenate([s.run(_abi.FP32C)[0] for s, _, _ in refs])
                             if fast is not None else None)
             else:
-                cmp_head = np.concatenate([pick(h, cols, nz) for h, (_, cols, _) in zip(head_pts, refs)])
-                cmp_fast = (np.concatenate([pick(h, cols, nz) for h, (_, cols, _) in zip(fast_pts, refs)])
-                            if fast_pts is not None else None)
+                cmp_head = np.concatenate(head_pts)
+                cmp_fast = np.concatenate(fast_pts) if fast_pts is not None else None
             p64 = np.concatenate([p for _, _, p in refs])
             fp64 = {"points_per_s": rate64, "points": npts64, "subset": subset,
                     "speedup_vs_fp64": {head_name: value / world / rate64},
@@ -898,12 +913,12 @@ def ours(args, rank, world, local):
                 for s, _, _ in refs:
                     s.close()
         peak_tflops = fp32_peak(dev)
-        # algorithmic flops of the relax: per-scan flops per force evaluation,
-        # weighted by each scan's share of the pair terms (points x terms)
-        wts = np.array([d.n_points * max(d.c.n_atoms, 1) for d in descs], dtype=float)
+        # algorithmic flops of the relax: every scan's force evaluations (from
+        # its point records) x its flops per evaluation
+        evs = record_evals(outs)
         fpe = np.array([term_flops(d) for d in descs], dtype=float)
         ms_relax = ms_part["relax"]
-        relax_flops = st.force_evals * float((wts * fpe).sum() / wts.sum()) if fpe.any() else 0.0
+        relax_flops = float((evs * fpe).sum())
         kname = "relaxdf_kernel + repair64_kernel" if head == _abi.DF else "relax32_kernel"
         if fpe.any():
             relax_line = fp32_roofline(relax_flops / (ms_relax / 1000.0) / 1e12, peak_tflops, {
@@ -917,20 +932,24 @@ def ours(args, rank, world, local):
                 "kernel_ms_source": ("events recorded inside the timed graph replays"
                                      if step.external else
                                      "events around the same launches (no external graph events)"),
-                "flops_per_force_eval": float((wts * fpe).sum() / wts.sum()),
-                "force_evals": int(st.force_evals)})
+                "flops_per_force_eval": relax_flops / evs.sum(),
+                "force_evals": int(evs.sum()),
+                "force_evals_source": "FIRE steps of every point record x evaluations per step, "
+                                      "plus the output evaluation (the kernel's own counter, which "
+                                      "also counts re-relaxed columns' evaluations: "
+                                      f"{int(st.force_evals)})"})
             if head == _abi.DF:
                 # the kernel computes in double-float: its algorithmic work is
                 # the FP32 operations of the double-float term algorithms
                 fpe_df = np.array([term_flops(d, table=DF_TABLE) for d in descs], dtype=float)
-                df_per_eval = float((wts * fpe_df).sum() / wts.sum())
+                df_flops = float((evs * fpe_df).sum())
                 fp64_equiv = relax_flops / (ms_relax / 1000.0) / 1e12
-                relax_line["achieved"] = st.force_evals * df_per_eval / (ms_relax / 1000.0) / 1e12
+                relax_line["achieved"] = df_flops / (ms_relax / 1000.0) / 1e12
                 relax_line["frac"] = relax_line["achieved"] / peak_tflops
-                relax_line["flops_per_force_eval"] = df_per_eval
+                relax_line["flops_per_force_eval"] = df_flops / evs.sum()
                 relax_line["flops_source"] = DF_TABLE_TEXT
                 relax_line["fp64_equivalent"] = {
-                    "flops_per_force_eval": float((wts * fpe).sum() / wts.sum()),
+                    "flops_per_force_eval": relax_flops / evs.sum(),
                     "achieved_tflops": fp64_equiv,
                     "vs_fp64_peak_nominal": fp64_equiv / FP64_PEAK_NOMINAL_TFLOPS,
                     "note": "the FP64 expressions' flops (LJ 25, Morse 29, Coulomb 20 per term) "
@@ -991,7 +1010,7 @@ def ours(args, rank, world, local):
                                                    "note": "FP32 per-term Jacobians and parameter "
                                                            "derivatives, FP64 3x3 solve per point"}))
         if fast is not None and fpe.any():
-            f32 = fast["force_evals"] * float((wts * fpe).sum() / wts.sum())
+            f32 = float((record_evals(outs32) * fpe).sum())
             rooflines.append((fast["ms_per_step"], fp32_roofline(
                 f32 / (fast["ms_per_step"] / 1000.0) / 1e12, peak_tflops,
                 {"kernel": "relax32_kernel (MAFM_FP32C, the fast path)",
