@@ -166,7 +166,7 @@ typedef struct mafm_point {
 } mafm_point;
 
 typedef struct mafm_run_opts {
-    int32_t precision;          /* MAFM_FP64 or MAFM_FP32C */
+    int32_t precision;          /* MAFM_FP64, MAFM_FP32C or MAFM_DF */
     int32_t lanes_per_column;   /* FP32C: 1,2,4,8,16,32 lanes share a column; 0 = default
                                    (from the column count; mafm_autotune measures).
                                    MAFM_DF: 1,2,4,8 lanes share a column's terms; 0 =
